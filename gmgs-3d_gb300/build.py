@@ -1,0 +1,76 @@
+"""Build libgmgs.so (sm_103a) in-tree with nvcc; no CMake, no torch.
+
+    python gmgs-3d_gb300/build.py [--debug] [--jobs N]
+
+Each .cu translation unit compiles in parallel into _build/, then one shared
+library is linked into gmgs-3d_gb300/gmgs/libgmgs.so.
+"""
+from __future__ import annotations
+
+import argparse
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+ROOT = PKG.parent
+CSRC = PKG / "csrc"
+BUILD = ROOT / "_build" / "gmgs"
+LIB = PKG / "gmgs" / "libgmgs.so"
+SOURCES = ["api.cu", "setup.cu", "operators.cu", "solver.cu", "post.cu", "fine.cu"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and Path(cand).exists():
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def flags(debug: bool) -> list[str]:
+    f = ["-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", str(ROOT / "include"), "-I", str(CSRC),
+         "--expt-relaxed-constexpr", "-Xptxas", "-v" if os.environ.get("GMGS_PTXAS_V") else "-O3"]
+    f += ["-O0", "-g", "-DGMGS_CHECKED"] if debug else ["-O3"]
+    return ARCH + f
+
+
+def compile_one(src: str, debug: bool) -> Path:
+    out = BUILD / (Path(src).stem + ".o")
+    srcp = CSRC / src
+    deps = [srcp] + list(CSRC.glob("*.cuh")) + [ROOT / "include" / "gmgs.h"]
+    if out.exists() and all(out.stat().st_mtime >= d.stat().st_mtime for d in deps) and not debug:
+        return out
+    cmd = [nvcc(), *flags(debug), "-c", str(srcp), "-o", str(out)]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"nvcc failed for {src}:\n{res.stdout}\n{res.stderr}")
+    if os.environ.get("GMGS_PTXAS_V"):
+        sys.stderr.write(res.stderr)
+    return out
+
+
+def build(debug: bool = False, jobs: int | None = None) -> Path:
+    BUILD.mkdir(parents=True, exist_ok=True)
+    srcs = [s for s in SOURCES if (CSRC / s).exists()]
+    with cf.ThreadPoolExecutor(max_workers=jobs or min(8, len(srcs))) as ex:
+        objs = list(ex.map(lambda s: compile_one(s, debug), srcs))
+    newest = max(o.stat().st_mtime for o in objs)
+    if LIB.exists() and LIB.stat().st_mtime >= newest and not debug:
+        return LIB
+    cmd = [nvcc(), *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcusolver", "-lcudart"]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
+    return LIB
+
+
+if __name__ == "__main__":
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--debug", action="store_true")
+    ap.add_argument("--jobs", type=int, default=None)
+    a = ap.parse_args()
+    print(build(a.debug, a.jobs))

@@ -1,0 +1,218 @@
+// Internal definitions of libgmgs: dense per-level node grids on the GPU.
+//
+// Layout in HBM.  Level l has ny x nx x nz (padded) elements and
+// (ny+1) x (nx+1) x (nz+1) nodes.  Nodes live in a dense slot grid with a
+// one-node zero halo on every side, y fastest (the reference's column-major
+// (y, x, z) order, src/common/DiscretizeDesignDomain.m:76):
+//     slot(iy, ix, iz) = ((iz + 1) * px + (ix + 1)) * py + (iy + 1)
+// An element (ey, ex, ez) shares the slot of its lowest-index node, so the 8
+// elements around node n are the slots n - {0,1} * {1, py, py*px}.
+// Vectors are stored as three component planes of `slots` entries (SoA).
+// Every vector is zero on halo and non-solid slots, so stencils need no
+// bounds checks.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "gmgs.h"
+
+namespace gmgs {
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+struct Error : std::runtime_error {
+    int status;
+    Error(int s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+
+#define GMGS_CUDA(call)                                                              \
+    do {                                                                             \
+        cudaError_t e_ = (call);                                                     \
+        if (e_ != cudaSuccess) {                                                     \
+            throw ::gmgs::Error(e_ == cudaErrorMemoryAllocation ? GMGS_ERR_OUT_OF_MEMORY \
+                                                                : GMGS_ERR_CUDA,     \
+                                std::string(#call) + ": " + cudaGetErrorString(e_)); \
+        }                                                                            \
+    } while (0)
+
+// Record a kernel launch: check the launch error and count it.
+#define GMGS_LAUNCHED(ctx)                                                           \
+    do {                                                                             \
+        cudaError_t e_ = cudaGetLastError();                                         \
+        if (e_ != cudaSuccess)                                                       \
+            throw ::gmgs::Error(GMGS_ERR_CUDA, std::string("kernel launch: ") +      \
+                                                   cudaGetErrorString(e_));          \
+        ++(ctx).launches;                                                            \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// grid geometry
+// ---------------------------------------------------------------------------
+struct Grid {
+    int ny = 0, nx = 0, nz = 0;   // elements (padded)
+    int py = 0, px = 0, pz = 0;   // slot pitches, halo included
+    int64_t slots = 0;
+
+    static Grid make(int ny, int nx, int nz) {
+        Grid g;
+        g.ny = ny; g.nx = nx; g.nz = nz;
+        g.py = ((ny + 3) + 7) / 8 * 8;     // rows start on 32/64-byte boundaries
+        g.px = nx + 3;
+        g.pz = nz + 3;
+        g.slots = (int64_t)g.py * g.px * g.pz;
+        return g;
+    }
+    __host__ __device__ __forceinline__ int64_t slot(int iy, int ix, int iz) const {
+        return ((int64_t)(iz + 1) * px + (ix + 1)) * py + (iy + 1);
+    }
+    __host__ __device__ __forceinline__ int64_t sx() const { return py; }
+    __host__ __device__ __forceinline__ int64_t sz() const { return (int64_t)py * px; }
+};
+
+// Local node k of an element sits at (iy + CY[k], ix + CX[k], iz + CZ[k]) from the
+// element's lowest-index node: node 1 = (iy+1, ix, iz), 2 = (iy+1, ix+1, iz),
+// 3 = (iy, ix+1, iz), 4 = (iy, ix, iz), 5..8 the same at iz+1
+// (src/common/DiscretizeDesignDomain.m:80).
+__host__ __device__ constexpr int corner_y(int k) { return (k & 3) < 2 ? 1 : 0; }
+__host__ __device__ constexpr int corner_x(int k) { return ((k & 3) == 1 || (k & 3) == 2) ? 1 : 0; }
+__host__ __device__ constexpr int corner_z(int k) { return k >> 2; }
+__host__ __device__ constexpr int corner_of(int dy, int dx, int dz) {
+    return (dy ? (dx ? 1 : 0) : (dx ? 2 : 3)) + 4 * dz;
+}
+
+// node flag bits
+enum : uint8_t { NF_SOLID = 1, NF_FIX_X = 2, NF_FIX_Y = 4, NF_FIX_Z = 8 };
+
+// ---------------------------------------------------------------------------
+// device-side views passed to kernels by value
+// ---------------------------------------------------------------------------
+template <typename T>
+struct LevelView {
+    Grid g;
+    const uint8_t* emask;    // element solid / non-empty
+    const uint8_t* nflag;    // node flags
+    const int32_t* etype;    // -1 void, 0 universal (Kc), k>0 -> Ks[k-1]; null = all universal
+    const T* Ks;             // per-element matrices, 576 each, row = output DOF
+    const T* escale;         // finest-level element scale (density extension) or null
+    const T* diag;           // 3 planes
+    T omega;
+};
+
+// ---------------------------------------------------------------------------
+// host-side level storage
+// ---------------------------------------------------------------------------
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    DevBuf(DevBuf&& o) noexcept : p(o.p), bytes(o.bytes) { o.p = nullptr; o.bytes = 0; }
+    DevBuf& operator=(DevBuf&& o) noexcept {
+        if (this != &o) { release(); p = o.p; bytes = o.bytes; o.p = nullptr; o.bytes = 0; }
+        return *this;
+    }
+    ~DevBuf() { release(); }
+    void release() { if (p) cudaFree(p); p = nullptr; bytes = 0; }
+    template <typename T> T* as() const { return static_cast<T*>(p); }
+};
+
+struct Level {
+    Grid g;
+    int64_t n_elem = 0, n_node = 0;
+    int state = 0;            // reference storingState: 0 uniform, 1 per element, 2 unique + universal
+    int64_t nK = 0;           // per-element matrices held
+    double kscale = 1.0;      // universal matrix = Ke0 * kscale (SetupSolver.m:37)
+    DevBuf emask, nflag, etype, escale64, escale32;
+    DevBuf Ks64, Ks32;
+    DevBuf kslot;             // slot of the coarse element owning Ks[k]
+    DevBuf diag64, diag32;
+    DevBuf node_slot;         // compact node id -> slot (int32), reference nodMapBack order
+    DevBuf elem_slot;         // compact element id -> slot (int32), eleMapBack order
+    DevBuf node_count;        // finest level: solid elements per node (numNod2ElesVec_)
+    // V-cycle work vectors (3 planes each), precision of the V-cycle
+    DevBuf vr, vrp, vdx, vx, vy;
+};
+
+struct Ctx {
+    cudaStream_t stream = nullptr;
+    int64_t launches = 0;
+    int num_sms = 148;
+};
+
+// ---------------------------------------------------------------------------
+// kernels and launchers (operators.cu, setup.cu, post.cu)
+// ---------------------------------------------------------------------------
+constexpr int KE = 576;
+
+// uniform element matrices in constant memory: [0] = Ke0 (FP64), [1] = Ke0 (FP32)
+void upload_ke0(const double* ke0_rowmajor);
+
+template <typename T> LevelView<T> view(const Level& L, double omega);
+
+// y = K_l x, fixed rows zeroed (AtX.m:1-58).  Tin/Tout let the mixed path read
+// FP64 CG vectors and compute in FP32.
+template <typename Tc, typename Tin, typename Tout>
+void launch_matvec(Ctx& c, const LevelView<Tc>& lv, const Tin* x, Tout* y, double kscale);
+
+// dx = (omega r) / d  (JacobiSmoother.m:5)
+template <typename Tr, typename Td, typename Tx>
+void launch_jacobi_dx(Ctx& c, const Grid& g, const Td* diag, double omega, const Tr* r, Tx* dx);
+// x += dx (elementwise over 3 planes)
+template <typename T, typename U>
+void launch_add(Ctx& c, int64_t n, T* x, const U* dx);
+// r -= y
+template <typename T, typename U>
+void launch_sub(Ctx& c, int64_t n, T* r, const U* y);
+// out = a (conversion copy)
+template <typename T, typename U>
+void launch_copy(Ctx& c, int64_t n, T* out, const U* a);
+// out = a - b
+template <typename T>
+void launch_diff(Ctx& c, int64_t n, T* out, const T* a, const T* b);
+
+// restriction r_c = P^T r_f (RestrictResidual.m) and prolongation with the
+// post-smoothing term x_f = (dx + P x_c) + (omega r') / d (Vcycle.m:29-32)
+template <typename T>
+void launch_restrict(Ctx& c, const Grid& gf, const Grid& gc, const uint8_t* nflag_c,
+                     const T* rf, T* rc);
+template <typename T>
+void launch_prolong_post(Ctx& c, const Grid& gf, const Grid& gc, const uint8_t* nflag_f,
+                         const T* diag_f, double omega, const T* xc, const T* dx,
+                         const T* rp, T* xf, bool zero_fixed);
+
+// deterministic dot product: out[0] = sum a*b over n entries (FP64 accumulate)
+struct DotScratch { double* partials; unsigned int* ticket; int blocks; };
+template <typename Ta, typename Tb>
+void launch_dot(Ctx& c, const DotScratch& s, int64_t n, const Ta* a, const Tb* b, double* out);
+
+// CG updates.  scal: device scalars (see solver.cu)
+// cur_first = (r.z slot) | (first iteration << 1)
+template <typename Tz>
+void launch_p_update(Ctx& c, int64_t n, const Tz* z, double* p, const double* scal, int cur_first);
+template <typename Tq>
+void launch_xr_update(Ctx& c, int64_t n, double* x, double* r, const double* p, const Tq* q,
+                      const double* scal, int cur);
+
+// coarsest level: gather free DOFs, dense GEMV with the inverse, scatter back
+template <typename T>
+void launch_gather(Ctx& c, int64_t n, const int32_t* idx, const T* src, double* dst);
+template <typename T>
+void launch_scatter(Ctx& c, int64_t n, const int32_t* idx, const double* src, T* dst);
+void launch_gemv(Ctx& c, int n, const double* A, const double* x, double* y);
+
+// compact <-> dense (interleaved 3-vectors)
+template <typename T>
+void launch_compact_to_dense(Ctx& c, int64_t nn, int64_t slots, const int32_t* node_slot,
+                             const double* src, T* dst);
+template <typename T>
+void launch_dense_to_compact(Ctx& c, int64_t nn, int64_t slots, const int32_t* node_slot,
+                             const T* src, double* dst);
+
+}  // namespace gmgs

@@ -1,0 +1,855 @@
+// Solver setup on the GPU: finest discretisation, 2x2x2 hierarchy, Galerkin
+// coarse element matrices, Jacobi diagonals, boundary conditions, coarse fixed
+// DOFs and the coarsest-level factorisation.
+//
+// Reference: src/common/DiscretizeDesignDomain.m:29-116,
+// src/kernel/BuildingMeshHierarchy.m:8-142, src/kernel/SetupSolver.m:9-259,
+// src/kernel/DirectlyAssembleStifnessMatrix.m:24-34,
+// src/common/ApplyBoundaryCondition.m:7-23.
+#include <cublas_api.h>
+#include <cusolverDn.h>
+
+#include <algorithm>
+#include <cmath>
+#include <unordered_map>
+
+#include "setup.cuh"
+
+namespace gmgs {
+
+// ---------------------------------------------------------------------------
+// host FEM math (SetupStiffnessMatrix.m, ElementElasticityMatrix.m,
+// ElementStrainMatrix.m, GaussianIntegral.m, ShapeFunction.m,
+// DeShapeFunction.m, GetCartesianStress.m:44-73)
+// ---------------------------------------------------------------------------
+static const double kGauss = 0.577350269189626;   // GaussianIntegral.m:11 writes 15 digits
+static const int kSign[8][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1},
+                                {-1, -1, 1},  {1, -1, 1},  {1, 1, 1},  {-1, 1, 1}};
+
+static void hooke(double E, double nu, double S[6][6]) {
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) S[i][j] = 0;
+    const double c1 = (1 + nu) * (1 - 2 * nu), c2 = 2 * (1 + nu);
+    S[0][0] = E * (1 - nu) / c1;
+    S[0][1] = E * nu / c1;
+    S[0][2] = S[0][1];
+    S[1][0] = S[0][1]; S[1][1] = S[0][0]; S[1][2] = S[1][0];
+    S[2][0] = S[0][2]; S[2][1] = S[1][2]; S[2][2] = S[1][1];
+    S[3][3] = E / c2; S[4][4] = S[3][3]; S[5][5] = S[4][4];
+}
+
+static bool invert(int n, const double* A, double* Ainv) {
+    std::vector<double> M(A, A + n * n), I(n * n, 0.0);
+    for (int i = 0; i < n; ++i) I[i * n + i] = 1;
+    for (int c = 0; c < n; ++c) {
+        int piv = c;
+        for (int r = c + 1; r < n; ++r)
+            if (std::fabs(M[r * n + c]) > std::fabs(M[piv * n + c])) piv = r;
+        if (M[piv * n + c] == 0) return false;
+        if (piv != c)
+            for (int k = 0; k < n; ++k) { std::swap(M[c * n + k], M[piv * n + k]); std::swap(I[c * n + k], I[piv * n + k]); }
+        const double d = M[c * n + c];
+        for (int k = 0; k < n; ++k) { M[c * n + k] /= d; I[c * n + k] /= d; }
+        for (int r = 0; r < n; ++r) {
+            if (r == c) continue;
+            const double f = M[r * n + c];
+            if (f == 0) continue;
+            for (int k = 0; k < n; ++k) { M[r * n + k] -= f * M[c * n + k]; I[r * n + k] -= f * I[c * n + k]; }
+        }
+    }
+    std::copy(I.begin(), I.end(), Ainv);
+    return true;
+}
+
+// B (48x24) and the Jacobian determinants of a box element with edge lengths
+// (dx, dy, dz); node 1 at (-x, -y, -z) (DiscretizeDesignDomain.m:96).
+static void strain_matrix(const double ele[3], double B[48][24], double detJ[8]) {
+    double X[8][3];
+    for (int k = 0; k < 8; ++k)
+        for (int d = 0; d < 3; ++d) X[k][d] = (kSign[k][d] + 1) * 0.5 * ele[d];
+    for (int g = 0; g < 48; ++g)
+        for (int j = 0; j < 24; ++j) B[g][j] = 0;
+    for (int g = 0; g < 8; ++g) {
+        const double s = kGauss * kSign[g][0], t = kGauss * kSign[g][1], p = kGauss * kSign[g][2];
+        double dN[3][8];
+        for (int k = 0; k < 8; ++k) {
+            const double fs = 1 + s * kSign[k][0], ft = 1 + t * kSign[k][1], fp = 1 + p * kSign[k][2];
+            dN[0][k] = 0.125 * kSign[k][0] * ft * fp;
+            dN[1][k] = 0.125 * kSign[k][1] * fs * fp;
+            dN[2][k] = 0.125 * kSign[k][2] * fs * ft;
+        }
+        double J[9], Ji[9];
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) {
+                double v = 0;
+                for (int k = 0; k < 8; ++k) v += dN[a][k] * X[k][b];
+                J[a * 3 + b] = v;
+            }
+        detJ[g] = J[0] * (J[4] * J[8] - J[5] * J[7]) - J[1] * (J[3] * J[8] - J[5] * J[6]) +
+                  J[2] * (J[3] * J[7] - J[4] * J[6]);
+        invert(3, J, Ji);
+        for (int k = 0; k < 8; ++k) {
+            double d[3];
+            for (int a = 0; a < 3; ++a) d[a] = Ji[a * 3 + 0] * dN[0][k] + Ji[a * 3 + 1] * dN[1][k] + Ji[a * 3 + 2] * dN[2][k];
+            const int r = 6 * g, c = 3 * k;
+            B[r + 0][c + 0] = d[0];
+            B[r + 1][c + 1] = d[1];
+            B[r + 2][c + 2] = d[2];
+            B[r + 3][c + 1] = d[2]; B[r + 3][c + 2] = d[1];
+            B[r + 4][c + 0] = d[2]; B[r + 4][c + 2] = d[0];
+            B[r + 5][c + 0] = d[1]; B[r + 5][c + 1] = d[0];
+        }
+    }
+}
+
+void element_stiffness(double E, double nu, const double ele[3], double Ke[576]) {
+    static double B[48][24];
+    double detJ[8], S[6][6];
+    strain_matrix(ele, B, detJ);
+    hooke(E, nu, S);
+    // (B^T (D .* wgt)) B, the reference's evaluation order (SetupStiffnessMatrix.m:22)
+    std::vector<double> BtDw(24 * 48, 0.0);
+    for (int i = 0; i < 24; ++i)
+        for (int g = 0; g < 8; ++g)
+            for (int b = 0; b < 6; ++b) {
+                double v = 0;
+                for (int a = 0; a < 6; ++a) v += B[6 * g + a][i] * S[a][b];
+                BtDw[i * 48 + 6 * g + b] = v * detJ[g];
+            }
+    for (int i = 0; i < 24; ++i)
+        for (int j = 0; j < 24; ++j) {
+            double v = 0;
+            for (int r = 0; r < 48; ++r) v += BtDw[i * 48 + r] * B[r][j];
+            Ke[i * 24 + j] = v;
+        }
+}
+
+void stress_matrices(double E, double nu, const double ele[3], double Mn[48 * 24], double Mg[48 * 24]) {
+    static double B[48][24];
+    double detJ[8], S[6][6];
+    strain_matrix(ele, B, detJ);
+    hooke(E, nu, S);
+    double DB[48][24];
+    for (int g = 0; g < 8; ++g)
+        for (int a = 0; a < 6; ++a)
+            for (int j = 0; j < 24; ++j) {
+                double v = 0;
+                for (int b = 0; b < 6; ++b) v += S[a][b] * B[6 * g + b][j];
+                DB[6 * g + a][j] = v;
+            }
+    // OTP = inv(kron(N, I6)) = kron(inv(N), I6)   (GetCartesianStress.m:44-73)
+    double N[64], Ni[64];
+    for (int g = 0; g < 8; ++g) {
+        const double s = kGauss * kSign[g][0], t = kGauss * kSign[g][1], p = kGauss * kSign[g][2];
+        for (int k = 0; k < 8; ++k)
+            N[g * 8 + k] = 0.125 * (1 + s * kSign[k][0]) * (1 + t * kSign[k][1]) * (1 + p * kSign[k][2]);
+    }
+    invert(8, N, Ni);
+    for (int k = 0; k < 8; ++k)
+        for (int a = 0; a < 6; ++a)
+            for (int j = 0; j < 24; ++j) {
+                double v = 0;
+                for (int g = 0; g < 8; ++g) v += Ni[k * 8 + g] * DB[6 * g + a][j];
+                Mn[(6 * k + a) * 24 + j] = v;
+                Mg[(6 * k + a) * 24 + j] = DB[6 * k + a][j];
+            }
+}
+
+// ---------------------------------------------------------------------------
+// exclusive scan of int32 counts (in place), deterministic three-phase
+// ---------------------------------------------------------------------------
+constexpr int SCAN_T = 1024, SCAN_ITEMS = 4;
+constexpr int SCAN_TILE = SCAN_T * SCAN_ITEMS;
+
+__global__ void k_scan_reduce(const int32_t* __restrict__ d, int64_t n, int64_t* __restrict__ bsum) {
+    __shared__ int64_t sh[32];
+    const int64_t base = blockIdx.x * (int64_t)SCAN_TILE;
+    int64_t s = 0;
+    for (int i = 0; i < SCAN_ITEMS; ++i) {
+        const int64_t k = base + i * SCAN_T + threadIdx.x;
+        if (k < n) s += d[k];
+    }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        s = sh[threadIdx.x];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (threadIdx.x == 0) bsum[blockIdx.x] = s;
+    }
+}
+
+__global__ void k_scan_blocks(int64_t* bsum, int64_t nb, int64_t* total) {
+    // single thread block: sequential chunks, exclusive scan of block sums
+    __shared__ int64_t carry;
+    __shared__ int64_t sh[SCAN_T];
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int64_t b0 = 0; b0 < nb; b0 += SCAN_T) {
+        const int64_t k = b0 + threadIdx.x;
+        const int64_t v = k < nb ? bsum[k] : 0;
+        sh[threadIdx.x] = v;
+        __syncthreads();
+        for (int o = 1; o < SCAN_T; o <<= 1) {
+            int64_t t = threadIdx.x >= o ? sh[threadIdx.x - o] : 0;
+            __syncthreads();
+            sh[threadIdx.x] += t;
+            __syncthreads();
+        }
+        if (k < nb) bsum[k] = carry + sh[threadIdx.x] - v;
+        __syncthreads();
+        if (threadIdx.x == SCAN_T - 1) carry += sh[SCAN_T - 1];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void k_scan_apply(int32_t* __restrict__ d, int64_t n, const int64_t* __restrict__ bsum) {
+    __shared__ int64_t sh[SCAN_T];
+    const int64_t base = blockIdx.x * (int64_t)SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS;
+    int32_t v[SCAN_ITEMS];
+    int64_t s = 0;
+    for (int i = 0; i < SCAN_ITEMS; ++i) {
+        v[i] = base + i < n ? d[base + i] : 0;
+        s += v[i];
+    }
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 1; o < SCAN_T; o <<= 1) {
+        int64_t t = threadIdx.x >= o ? sh[threadIdx.x - o] : 0;
+        __syncthreads();
+        sh[threadIdx.x] += t;
+        __syncthreads();
+    }
+    int64_t run = bsum[blockIdx.x] + sh[threadIdx.x] - s;
+    for (int i = 0; i < SCAN_ITEMS; ++i) {
+        if (base + i < n) d[base + i] = (int32_t)run;
+        run += v[i];
+    }
+}
+
+int64_t exclusive_scan(Ctx& c, int32_t* d, int64_t n) {
+    const int64_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
+    DevBuf bs = dalloc((nb + 1) * sizeof(int64_t));
+    int64_t* bsum = bs.as<int64_t>();
+    k_scan_reduce<<<(unsigned)nb, SCAN_T, 0, c.stream>>>(d, n, bsum);
+    GMGS_LAUNCHED(c);
+    k_scan_blocks<<<1, SCAN_T, 0, c.stream>>>(bsum, nb, bsum + nb);
+    GMGS_LAUNCHED(c);
+    k_scan_apply<<<(unsigned)nb, SCAN_T, 0, c.stream>>>(d, n, bsum);
+    GMGS_LAUNCHED(c);
+    int64_t total = 0;
+    GMGS_CUDA(cudaMemcpyAsync(&total, bsum + nb, sizeof(int64_t), cudaMemcpyDeviceToHost, c.stream));
+    GMGS_CUDA(cudaStreamSynchronize(c.stream));
+    if (total > INT32_MAX) throw Error(GMGS_ERR_INVALID_ARGUMENT, "model too large for 32-bit compact ids");
+    return total;
+}
+
+DevBuf dalloc(size_t bytes) {
+    DevBuf b;
+    if (bytes == 0) bytes = 16;
+    GMGS_CUDA(cudaMalloc(&b.p, bytes));
+    b.bytes = bytes;
+    return b;
+}
+
+static int blocks_for(const Ctx& c, int64_t n) {
+    int64_t b = (n + 255) / 256;
+    const int64_t cap = (int64_t)c.num_sms * 32;
+    return (int)std::max<int64_t>(1, std::min(b, cap));
+}
+
+#define GRID_STRIDE(i, n) \
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (n); i += (int64_t)gridDim.x * blockDim.x)
+
+__device__ __forceinline__ void slot_coords(const Grid& g, int64_t s, int& iy, int& ix, int& iz) {
+    iy = (int)(s % g.py) - 1;
+    const int64_t r = s / g.py;
+    ix = (int)(r % g.px) - 1;
+    iz = (int)(r / g.px) - 1;
+}
+
+// ---------------------------------------------------------------------------
+// masks
+// ---------------------------------------------------------------------------
+// finest element mask from the (unpadded) occupancy; only 1 is solid (DiscretizeDesignDomain.m:68)
+__global__ void k_emask_l1(Grid g, const int32_t* __restrict__ occ, int nely, int nelx, int nelz,
+                           uint8_t* __restrict__ emask) {
+    GRID_STRIDE(s, g.slots) {
+        int iy, ix, iz;
+        slot_coords(g, s, iy, ix, iz);
+        uint8_t v = 0;
+        if (iy >= 0 && ix >= 0 && iz >= 0 && iy < nely && ix < nelx && iz < nelz)
+            v = occ[iy + (int64_t)nely * (ix + (int64_t)nelx * iz)] == 1;
+        emask[s] = v;
+    }
+}
+
+// coarse element = non-empty if any child is solid (BuildingMeshHierarchy.m:70).
+// kmode: 0 none, 1 "unique if a child is void" (SetupSolver.m:43-44),
+// 2 "unique if a non-void child is unique on the finer level" (SetupSolver.m:96-101),
+// 3 every non-empty element gets its own matrix (state 1).
+__global__ void k_coarsen(Grid gc, Grid gf, const uint8_t* __restrict__ emf, const int32_t* __restrict__ etf,
+                          int kmode, uint8_t* __restrict__ emc, int32_t* __restrict__ needK) {
+    GRID_STRIDE(s, gc.slots) {
+        int iy, ix, iz;
+        slot_coords(gc, s, iy, ix, iz);
+        uint8_t any = 0, allsolid = 1, kid_unique = 0;
+        if (iy >= 0 && ix >= 0 && iz >= 0 && iy < gc.ny && ix < gc.nx && iz < gc.nz) {
+            for (int j = 0; j < 8; ++j) {
+                const int64_t fs = gf.slot(2 * iy + (j & 1), 2 * ix + ((j >> 1) & 1), 2 * iz + (j >> 2));
+                const uint8_t m = emf[fs];
+                any |= m;
+                allsolid &= m;
+                if (m && etf && etf[fs] > 0) kid_unique = 1;
+            }
+        } else {
+            allsolid = 0;
+        }
+        emc[s] = any;
+        int32_t nk = 0;
+        if (any) {
+            if (kmode == 1) nk = !allsolid;
+            else if (kmode == 2) nk = kid_unique;
+            else if (kmode == 3) nk = 1;
+        }
+        if (needK) needK[s] = nk;
+    }
+}
+
+__global__ void k_node_flags(Grid g, const uint8_t* __restrict__ emask, uint8_t* __restrict__ nflag,
+                             int32_t* __restrict__ cnt) {
+    GRID_STRIDE(s, g.slots) {
+        int iy, ix, iz;
+        slot_coords(g, s, iy, ix, iz);
+        int n = 0;
+        if (iy >= 0 && ix >= 0 && iz >= 0 && iy <= g.ny && ix <= g.nx && iz <= g.nz) {
+            for (int e = 0; e < 8; ++e)
+                n += emask[s - (e & 1) - ((e >> 1) & 1) * g.sx() - (e >> 2) * g.sz()];
+        }
+        nflag[s] = n ? NF_SOLID : 0;
+        if (cnt) cnt[s] = n;
+    }
+}
+
+__global__ void k_flag_to_count(int64_t n, const uint8_t* __restrict__ f, uint8_t bit, int32_t* __restrict__ out) {
+    GRID_STRIDE(i, n) out[i] = (f[i] & bit) ? 1 : 0;
+}
+
+// slots with count 1 before the scan -> compact list (scan holds the exclusive prefix)
+__global__ void k_compact(int64_t n, const uint8_t* __restrict__ f, uint8_t bit, const int32_t* __restrict__ scan,
+                          int32_t* __restrict__ list) {
+    GRID_STRIDE(i, n) if (f[i] & bit) list[scan[i]] = (int32_t)i;
+}
+
+__global__ void k_etype(int64_t n, const uint8_t* __restrict__ emask, const int32_t* __restrict__ needK_scan,
+                        const int32_t* __restrict__ needK_flag, int32_t* __restrict__ etype,
+                        int32_t* __restrict__ kslot) {
+    GRID_STRIDE(i, n) {
+        int32_t t = -1;
+        if (emask[i]) {
+            const bool nk = needK_flag[i] != 0;
+            t = nk ? needK_scan[i] + 1 : 0;
+            if (nk) kslot[needK_scan[i]] = (int32_t)i;
+        }
+        etype[i] = t;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Galerkin coarse element matrices: Ks_c = sum_j P_j^T K_j P_j over solid
+// children j (SetupSolver.m:36-196 with the 81x24 trilinear table).
+// One block per coarse element, FP64.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double tri_w(int pos, int corner2) {
+    const int d = pos > corner2 ? pos - corner2 : corner2 - pos;
+    return d == 0 ? 1.0 : (d == 1 ? 0.5 : 0.0);
+}
+
+__global__ void __launch_bounds__(192) k_galerkin(Grid gc, Grid gf, const int32_t* __restrict__ kslot,
+                                                  const uint8_t* __restrict__ emf, const int32_t* __restrict__ etf,
+                                                  const double* __restrict__ Ksf, const double* __restrict__ ke0,
+                                                  double kscale_f, const double* __restrict__ escale_f,
+                                                  double* __restrict__ Ks_out) {
+    __shared__ double K[KE], T[KE], W[64];
+    const int64_t s = kslot[blockIdx.x];
+    int Ey, Ex, Ez;
+    slot_coords(gc, s, Ey, Ex, Ez);
+    double acc[3] = {0, 0, 0};    // 576 / 192 entries per thread
+    for (int j = 0; j < 8; ++j) {
+        const int dy = j & 1, dx = (j >> 1) & 1, dz = j >> 2;
+        const int64_t fs = gf.slot(2 * Ey + dy, 2 * Ex + dx, 2 * Ez + dz);
+        if (!emf[fs]) continue;       // uniform branch across the block
+        const int t = etf ? etf[fs] : 0;
+        const double sc = kscale_f * (escale_f ? escale_f[fs] : 1.0);
+        for (int i = threadIdx.x; i < KE; i += blockDim.x)
+            K[i] = t > 0 ? Ksf[(int64_t)(t - 1) * KE + i] : sc * ke0[i];
+        if (threadIdx.x < 64) {
+            const int q = threadIdx.x >> 3, b = threadIdx.x & 7;   // W[q][b]: corner b at child-local node q
+            W[threadIdx.x] = tri_w(dy + corner_y(q), 2 * corner_y(b)) * tri_w(dx + corner_x(q), 2 * corner_x(b)) *
+                             tri_w(dz + corner_z(q), 2 * corner_z(b));
+        }
+        __syncthreads();
+        // T = K P : T[r][3b+be] = sum_q K[r][3q+be] W[q][b]
+        for (int i = threadIdx.x; i < KE; i += blockDim.x) {
+            const int r = i / 24, col = i % 24, b = col / 3, be = col % 3;
+            double v = 0;
+            for (int q = 0; q < 8; ++q) v += K[r * 24 + 3 * q + be] * W[q * 8 + b];
+            T[i] = v;
+        }
+        __syncthreads();
+        // out += P^T T : out[3a+al][col] += sum_p W[p][a] T[3p+al][col]
+        for (int k = 0; k < 3; ++k) {
+            const int i = threadIdx.x + k * blockDim.x;
+            const int row = i / 24, col = i % 24, a = row / 3, al = row % 3;
+            double v = 0;
+            for (int p = 0; p < 8; ++p) v += W[p * 8 + a] * T[(3 * p + al) * 24 + col];
+            acc[k] += v;
+        }
+        __syncthreads();
+    }
+    for (int k = 0; k < 3; ++k) Ks_out[(int64_t)blockIdx.x * KE + threadIdx.x + k * blockDim.x] = acc[k];
+}
+
+// ---------------------------------------------------------------------------
+// Jacobi diagonal: sum of the element diagonals at each node (SetupSolver.m:204-244)
+// ---------------------------------------------------------------------------
+__global__ void k_diag(Grid g, const uint8_t* __restrict__ emask, const uint8_t* __restrict__ nflag,
+                       const int32_t* __restrict__ etype, const double* __restrict__ Ks, const double* __restrict__ ke0,
+                       double kscale, const double* __restrict__ escale, double* __restrict__ d) {
+    GRID_STRIDE(s, g.slots) {
+        double a[3] = {0, 0, 0};
+        if (nflag[s] & NF_SOLID) {
+            for (int e = 0; e < 8; ++e) {
+                const int A = e & 1, B = (e >> 1) & 1, C = e >> 2;
+                const int64_t es = s - A - B * g.sx() - C * g.sz();
+                if (!emask[es]) continue;
+                const int c = corner_of(A, B, C);
+                const int t = etype ? etype[es] : 0;
+                for (int al = 0; al < 3; ++al) {
+                    const int ii = (3 * c + al) * 24 + 3 * c + al;
+                    a[al] += t > 0 ? Ks[(int64_t)(t - 1) * KE + ii] : kscale * (escale ? escale[es] : 1.0) * ke0[ii];
+                }
+            }
+        }
+        d[s] = a[0];
+        d[s + g.slots] = a[1];
+        d[s + 2 * g.slots] = a[2];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// boundary conditions
+// ---------------------------------------------------------------------------
+__global__ void k_clear_fixed(int64_t n, uint8_t* f) {
+    GRID_STRIDE(i, n) f[i] &= NF_SOLID;
+}
+__global__ void k_set_fixed(int64_t n, const int32_t* __restrict__ ids, const int32_t* __restrict__ node_slot,
+                            uint8_t* __restrict__ f) {
+    GRID_STRIDE(i, n) f[node_slot[ids[i] - 1]] |= (NF_FIX_X | NF_FIX_Y | NF_FIX_Z);
+}
+__global__ void k_set_loads(int64_t n, const int32_t* __restrict__ ids, const double* __restrict__ fv,
+                            const int32_t* __restrict__ node_slot, int64_t S, double* __restrict__ F) {
+    GRID_STRIDE(i, n) {
+        const int64_t s = node_slot[ids[i] - 1];
+        F[s] = fv[3 * i];
+        F[s + S] = fv[3 * i + 1];
+        F[s + 2 * S] = fv[3 * i + 2];
+    }
+}
+// coarse fixed DOFs: restricted indicator != 0 (SetupSolver.m:247-254)
+__global__ void k_fixed_from_indicator(int64_t S, const double* __restrict__ ind, uint8_t* __restrict__ f) {
+    GRID_STRIDE(s, S) {
+        uint8_t v = f[s] & NF_SOLID;
+        if (v) {
+            if (ind[s] != 0.0) v |= NF_FIX_X;
+            if (ind[s + S] != 0.0) v |= NF_FIX_Y;
+            if (ind[s + 2 * S] != 0.0) v |= NF_FIX_Z;
+        }
+        f[s] = v;
+    }
+}
+__global__ void k_indicator(int64_t S, const uint8_t* __restrict__ f, double* __restrict__ ind) {
+    GRID_STRIDE(s, S) {
+        ind[s] = (f[s] & NF_FIX_X) ? 1.0 : 0.0;
+        ind[s + S] = (f[s] & NF_FIX_Y) ? 1.0 : 0.0;
+        ind[s + 2 * S] = (f[s] & NF_FIX_Z) ? 1.0 : 0.0;
+    }
+}
+
+// free DOFs of the coarsest level, node-major then component (reference freeDOFs order)
+__global__ void k_free_count(int64_t S, const uint8_t* __restrict__ f, int32_t* __restrict__ cnt) {
+    GRID_STRIDE(i, 3 * S) {
+        const int64_t s = i / 3;
+        const int comp = (int)(i % 3);
+        cnt[i] = (f[s] & NF_SOLID) && !(f[s] & (NF_FIX_X << comp));
+    }
+}
+__global__ void k_free_list(int64_t S, const uint8_t* __restrict__ f, const int32_t* __restrict__ scan,
+                            int32_t* __restrict__ idx) {
+    GRID_STRIDE(i, 3 * S) {
+        const int64_t s = i / 3;
+        const int comp = (int)(i % 3);
+        if ((f[s] & NF_SOLID) && !(f[s] & (NF_FIX_X << comp))) idx[scan[i]] = (int32_t)(s + comp * S);
+    }
+}
+
+// dense coarsest matrix on the free DOFs, K[row][col] = sum_e Ks_e(i, j) with
+// row = dof of local i, col = dof of local j (DirectlyAssembleStifnessMatrix.m:25-32).
+// Stored matrices have row = output DOF, so Ks_e(i, j) = M_e[j][i].
+// One thread per (free row, neighbour dof); deterministic element order.
+__global__ void k_assemble_coarsest(Grid g, int nf, const int32_t* __restrict__ freeidx, const int32_t* __restrict__ rank,
+                                    const uint8_t* __restrict__ emask, const int32_t* __restrict__ etype,
+                                    const double* __restrict__ Ks, const double* __restrict__ ke0, double kscale,
+                                    double* __restrict__ Kd) {
+    const int64_t total = (int64_t)nf * 81;
+    GRID_STRIDE(t, total) {
+        const int row = (int)(t / 81);
+        const int k = (int)(t % 81);
+        const int off = k / 3, be = k % 3;
+        const int oa = off % 3 - 1, ob = (off / 3) % 3 - 1, oc = off / 9 - 1;
+        const int64_t ri = freeidx[row];
+        const int64_t S = g.slots;
+        const int al = (int)(ri / S);
+        const int64_t n = ri % S;
+        const int64_t m = n + oa + ob * g.sx() + oc * g.sz();
+        const int col = rank[m + be * S];
+        if (col < 0) continue;
+        double v = 0;
+        for (int e = 0; e < 8; ++e) {
+            const int A = e & 1, B = (e >> 1) & 1, C = e >> 2;
+            const int64_t es = n - A - B * g.sx() - C * g.sz();
+            // element must also contain m: m - es in {0,1}^3
+            const int my = A + oa, mx = B + ob, mz = C + oc;
+            if (my < 0 || my > 1 || mx < 0 || mx > 1 || mz < 0 || mz > 1) continue;
+            if (!emask[es]) continue;
+            const int cn = corner_of(A, B, C), cm = corner_of(my, mx, mz);
+            const int t2 = etype ? etype[es] : 0;
+            const int ii = (3 * cm + be) * 24 + 3 * cn + al;
+            v += t2 > 0 ? Ks[(int64_t)(t2 - 1) * KE + ii] : kscale * ke0[ii];
+        }
+        Kd[(int64_t)row * nf + col] = v;
+    }
+}
+__global__ void k_rank_fill(int64_t n, int32_t* r) { GRID_STRIDE(i, n) r[i] = -1; }
+__global__ void k_rank_set(int64_t nf, const int32_t* __restrict__ idx, int32_t* __restrict__ r) {
+    GRID_STRIDE(i, nf) r[idx[i]] = (int32_t)i;
+}
+__global__ void k_symmetrize_lower(int n, double* A) {
+    const int64_t total = (int64_t)n * n;
+    GRID_STRIDE(t, total) {
+        const int i = (int)(t / n), j = (int)(t % n);
+        // column-major lower (i >= j) holds the result; write the upper mirror
+        if (i < j) A[(int64_t)j * n + i] = A[(int64_t)i * n + j];
+    }
+}
+
+__global__ void k_to_float(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
+    GRID_STRIDE(i, n) b[i] = (float)a[i];
+}
+__global__ void k_node_count_compact(int64_t nn, const int32_t* __restrict__ node_slot, const int32_t* __restrict__ cnt,
+                                     double* __restrict__ out) {
+    GRID_STRIDE(i, nn) out[i] = (double)cnt[node_slot[i]];
+}
+
+// ---------------------------------------------------------------------------
+// host orchestration
+// ---------------------------------------------------------------------------
+void build_levels(Model& M, const int32_t* occ_dev) {
+    Ctx& c = M.ctx;
+    const int L = M.num_levels;
+    if (occ_dev) {
+        M.levels.clear();
+        M.levels.resize(L);
+    } else {
+        // rebuild the coarse levels, keep the finest masks and element scale
+        for (int l = 1; l < L; ++l) M.levels[l] = Level();
+    }
+    for (int l = 0; l < L; ++l) {
+        Level& lv = M.levels[l];
+        lv.g = Grid::make(M.ny >> l, M.nx >> l, M.nz >> l);
+        lv.kscale = std::ldexp(1.0, l);   // Ke0 * eleSize_l / eleSize_1 (SetupSolver.m:37)
+        if (!lv.emask.p) lv.emask = dalloc(lv.g.slots);
+        if (!lv.nflag.p) lv.nflag = dalloc(lv.g.slots);
+    }
+    // finest masks
+    if (occ_dev) {
+        Level& lv = M.levels[0];
+        k_emask_l1<<<blocks_for(c, lv.g.slots), 256, 0, c.stream>>>(lv.g, occ_dev, M.nely, M.nelx, M.nelz,
+                                                                     lv.emask.as<uint8_t>());
+        GMGS_LAUNCHED(c);
+    }
+    // coarse masks + per-element matrix selection
+    for (int l = 1; l < L; ++l) {
+        Level& lv = M.levels[l];
+        Level& fv = M.levels[l - 1];
+        int kmode;
+        if (M.has_density) kmode = 3;
+        else if (l == 1 && L > 2) kmode = 1;        // SetupSolver.m:39-68
+        else if (l == 2 && L > 3) kmode = 2;        // SetupSolver.m:90-131
+        else kmode = 3;                              // state 1
+        lv.state = kmode == 3 ? 1 : 2;
+        DevBuf need = dalloc(lv.g.slots * sizeof(int32_t));
+        DevBuf need0 = dalloc(lv.g.slots * sizeof(int32_t));
+        k_coarsen<<<blocks_for(c, lv.g.slots), 256, 0, c.stream>>>(lv.g, fv.g, fv.emask.as<uint8_t>(),
+                                                                    fv.etype.as<int32_t>(), kmode,
+                                                                    lv.emask.as<uint8_t>(), need.as<int32_t>());
+        GMGS_LAUNCHED(c);
+        GMGS_CUDA(cudaMemcpyAsync(need0.p, need.p, lv.g.slots * sizeof(int32_t), cudaMemcpyDeviceToDevice, c.stream));
+        lv.nK = exclusive_scan(c, need.as<int32_t>(), lv.g.slots);
+        lv.etype = dalloc(lv.g.slots * sizeof(int32_t));
+        lv.kslot = dalloc(std::max<int64_t>(1, lv.nK) * sizeof(int32_t));
+        // etype: need0 holds the 0/1 flags, need the exclusive prefix
+        k_etype<<<blocks_for(c, lv.g.slots), 256, 0, c.stream>>>(
+            lv.g.slots, lv.emask.as<uint8_t>(), need.as<int32_t>(), need0.as<int32_t>(), lv.etype.as<int32_t>(),
+            lv.kslot.as<int32_t>());
+        GMGS_LAUNCHED(c);        GMGS_CUDA(cudaStreamSynchronize(c.stream));   // temporaries are freed at scope exit
+    }
+    // node flags, compact node maps, element counts
+    for (int l = 0; l < L; ++l) {
+        Level& lv = M.levels[l];
+        DevBuf cnt = dalloc(lv.g.slots * sizeof(int32_t));
+        k_node_flags<<<blocks_for(c, lv.g.slots), 256, 0, c.stream>>>(lv.g, lv.emask.as<uint8_t>(),
+                                                                       lv.nflag.as<uint8_t>(), cnt.as<int32_t>());
+        GMGS_LAUNCHED(c);
+        DevBuf sc = dalloc(lv.g.slots * sizeof(int32_t));
+        k_flag_to_count<<<blocks_for(c, lv.g.slots), 256, 0, c.stream>>>(lv.g.slots, lv.nflag.as<uint8_t>(), NF_SOLID,
+                                                                          sc.as<int32_t>());
+        GMGS_LAUNCHED(c);
+        lv.n_node = exclusive_scan(c, sc.as<int32_t>(), lv.g.slots);
+        lv.node_slot = dalloc(std::max<int64_t>(1, lv.n_node) * sizeof(int32_t));
+        k_compact<<<blocks_for(c, lv.g.slots), 256, 0, c.stream>>>(lv.g.slots, lv.nflag.as<uint8_t>(), NF_SOLID,
+                                                                    sc.as<int32_t>(), lv.node_slot.as<int32_t>());
+        GMGS_LAUNCHED(c);
+        // elements
+        k_flag_to_count<<<blocks_for(c, lv.g.slots), 256, 0, c.stream>>>(lv.g.slots, lv.emask.as<uint8_t>(), 1,
+                                                                          sc.as<int32_t>());
+        GMGS_LAUNCHED(c);
+        lv.n_elem = exclusive_scan(c, sc.as<int32_t>(), lv.g.slots);
+        lv.elem_slot = dalloc(std::max<int64_t>(1, lv.n_elem) * sizeof(int32_t));
+        k_compact<<<blocks_for(c, lv.g.slots), 256, 0, c.stream>>>(lv.g.slots, lv.emask.as<uint8_t>(), 1,
+                                                                    sc.as<int32_t>(), lv.elem_slot.as<int32_t>());
+        GMGS_LAUNCHED(c);
+        if (l == 0) {
+            lv.node_count = dalloc(std::max<int64_t>(1, lv.n_node) * sizeof(double));
+            k_node_count_compact<<<blocks_for(c, lv.n_node), 256, 0, c.stream>>>(
+                lv.n_node, lv.node_slot.as<int32_t>(), cnt.as<int32_t>(), lv.node_count.as<double>());
+            GMGS_LAUNCHED(c);
+        }
+        GMGS_CUDA(cudaStreamSynchronize(c.stream));
+    }
+    if (M.levels[0].n_elem == 0) throw Error(GMGS_ERR_NO_SOLID, "the occupancy has no solid voxel");
+    GMGS_CUDA(cudaStreamSynchronize(c.stream));
+}
+
+__global__ void k_escale(int64_t ne, const int32_t* __restrict__ elem_slot, const double* __restrict__ rho,
+                         double penal, double* __restrict__ esc) {
+    GRID_STRIDE(e, ne) esc[elem_slot[e]] = pow(rho[e], penal);
+}
+
+// Extension: finest element scale rho^penal; every coarse level then stores
+// one Galerkin matrix per element.
+void set_density_dev(Model& M, const double* rho_dev) {
+    Ctx& c = M.ctx;
+    Level& l0 = M.levels[0];
+    M.rho = dalloc(l0.n_elem * sizeof(double));
+    GMGS_CUDA(cudaMemcpyAsync(M.rho.p, rho_dev, l0.n_elem * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
+    l0.escale64 = dalloc(l0.g.slots * sizeof(double));
+    GMGS_CUDA(cudaMemsetAsync(l0.escale64.p, 0, l0.g.slots * sizeof(double), c.stream));
+    k_escale<<<blocks_for(c, l0.n_elem), 256, 0, c.stream>>>(l0.n_elem, l0.elem_slot.as<int32_t>(), M.rho.as<double>(),
+                                                             M.penal, l0.escale64.as<double>());
+    GMGS_LAUNCHED(c);
+    l0.escale32.release();
+    M.has_density = true;
+    build_levels(M, nullptr);
+    build_operators(M);
+}
+
+void build_operators(Model& M) {
+    Ctx& c = M.ctx;
+    const int L = M.num_levels;
+    double Ke[KE], KeT[KE];
+    element_stiffness(M.prm.youngs_modulus, M.prm.poisson_ratio, M.ele, Ke);
+    for (int i = 0; i < 24; ++i)
+        for (int j = 0; j < 24; ++j) KeT[i * 24 + j] = Ke[j * 24 + i];   // row = output DOF
+    std::copy(KeT, KeT + KE, M.ke0_rows);
+    upload_ke0(KeT);
+    M.ke0_dev = dalloc(KE * sizeof(double));
+    GMGS_CUDA(cudaMemcpyAsync(M.ke0_dev.p, KeT, KE * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    const double* ke0 = M.ke0_dev.as<double>();
+    // Galerkin matrices level by level
+    for (int l = 1; l < L; ++l) {
+        Level& lv = M.levels[l];
+        Level& fv = M.levels[l - 1];
+        lv.Ks64 = dalloc(std::max<int64_t>(1, lv.nK) * KE * sizeof(double));
+        if (lv.nK > 0) {
+            k_galerkin<<<(unsigned)lv.nK, 192, 0, c.stream>>>(
+                lv.g, fv.g, lv.kslot.as<int32_t>(), fv.emask.as<uint8_t>(), fv.etype.as<int32_t>(),
+                fv.Ks64.as<double>(), ke0, fv.kscale, l == 1 ? fv.escale64.as<double>() : nullptr,
+                lv.Ks64.as<double>());
+            GMGS_LAUNCHED(c);
+        }
+    }
+    // diagonals (levels 1..L-1) and FP32 copies for the mixed V-cycle
+    for (int l = 0; l < L; ++l) {
+        Level& lv = M.levels[l];
+        if (l < L - 1) {
+            lv.diag64 = dalloc(3 * lv.g.slots * sizeof(double));
+            k_diag<<<blocks_for(c, lv.g.slots), 256, 0, c.stream>>>(
+                lv.g, lv.emask.as<uint8_t>(), lv.nflag.as<uint8_t>(), lv.etype.as<int32_t>(), lv.Ks64.as<double>(),
+                ke0, lv.kscale, l == 0 ? lv.escale64.as<double>() : nullptr, lv.diag64.as<double>());
+            GMGS_LAUNCHED(c);
+        }
+        if (M.prm.precision == GMGS_MIXED) {
+            if (lv.nK > 0 && l < L - 1) {
+                lv.Ks32 = dalloc(lv.nK * KE * sizeof(float));
+                k_to_float<<<blocks_for(c, lv.nK * KE), 256, 0, c.stream>>>(lv.nK * KE, lv.Ks64.as<double>(),
+                                                                             lv.Ks32.as<float>());
+                GMGS_LAUNCHED(c);
+            }
+            if (l < L - 1) {
+                lv.diag32 = dalloc(3 * lv.g.slots * sizeof(float));
+                k_to_float<<<blocks_for(c, 3 * lv.g.slots), 256, 0, c.stream>>>(3 * lv.g.slots, lv.diag64.as<double>(),
+                                                                                 lv.diag32.as<float>());
+                GMGS_LAUNCHED(c);
+            }
+            if (l == 0 && lv.escale64.p) {
+                lv.escale32 = dalloc(lv.g.slots * sizeof(float));
+                k_to_float<<<blocks_for(c, lv.g.slots), 256, 0, c.stream>>>(lv.g.slots, lv.escale64.as<double>(),
+                                                                             lv.escale32.as<float>());
+                GMGS_LAUNCHED(c);
+            }
+        }
+    }
+    GMGS_CUDA(cudaStreamSynchronize(c.stream));
+}
+
+void apply_bc(Model& M, const int32_t* fixed, int64_t nfixed, const double* loads, int64_t nload) {
+    Ctx& c = M.ctx;
+    Level& lv = M.levels[0];
+    const int64_t nn = lv.n_node;
+    // host-side validation and "later duplicate wins" (ApplyBoundaryCondition.m:9)
+    std::vector<int32_t> fid(fixed, fixed + nfixed);
+    for (int32_t v : fid)
+        if (v < 1 || v > nn) throw Error(GMGS_ERR_INVALID_ARGUMENT, "fixed node id out of range");
+    std::unordered_map<int64_t, int64_t> last;
+    last.reserve((size_t)nload * 2);
+    for (int64_t i = 0; i < nload; ++i) {
+        const double idd = loads[4 * i];
+        if (!(idd >= 1 && idd <= (double)nn) || idd != std::floor(idd))
+            throw Error(GMGS_ERR_INVALID_ARGUMENT, "load node id out of range");
+        for (int k = 1; k < 4; ++k)
+            if (!std::isfinite(loads[4 * i + k])) throw Error(GMGS_ERR_NONFINITE, "non-finite load");
+        last[(int64_t)idd] = i;
+    }
+    std::vector<int32_t> lid;
+    std::vector<double> lval;
+    lid.reserve(last.size());
+    lval.reserve(3 * last.size());
+    for (int64_t i = 0; i < nload; ++i) {
+        const int64_t id = (int64_t)loads[4 * i];
+        if (last[id] != i) continue;
+        lid.push_back((int32_t)id);
+        for (int k = 1; k < 4; ++k) lval.push_back(loads[4 * i + k]);
+    }
+    DevBuf dfix = dalloc(std::max<int64_t>(1, nfixed) * sizeof(int32_t));
+    DevBuf dlid = dalloc(std::max<size_t>(1, lid.size()) * sizeof(int32_t));
+    DevBuf dlv = dalloc(std::max<size_t>(1, lval.size()) * sizeof(double));
+    GMGS_CUDA(cudaMemcpyAsync(dfix.p, fid.data(), nfixed * sizeof(int32_t), cudaMemcpyHostToDevice, c.stream));
+    GMGS_CUDA(cudaMemcpyAsync(dlid.p, lid.data(), lid.size() * sizeof(int32_t), cudaMemcpyHostToDevice, c.stream));
+    GMGS_CUDA(cudaMemcpyAsync(dlv.p, lval.data(), lval.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    k_clear_fixed<<<blocks_for(c, lv.g.slots), 256, 0, c.stream>>>(lv.g.slots, lv.nflag.as<uint8_t>());
+    GMGS_LAUNCHED(c);
+    k_set_fixed<<<blocks_for(c, nfixed), 256, 0, c.stream>>>(nfixed, dfix.as<int32_t>(), lv.node_slot.as<int32_t>(),
+                                                              lv.nflag.as<uint8_t>());
+    GMGS_LAUNCHED(c);
+    if (!M.F.p) M.F = dalloc(3 * lv.g.slots * sizeof(double));
+    GMGS_CUDA(cudaMemsetAsync(M.F.p, 0, 3 * lv.g.slots * sizeof(double), c.stream));
+    k_set_loads<<<blocks_for(c, (int64_t)lid.size()), 256, 0, c.stream>>>(
+        (int64_t)lid.size(), dlid.as<int32_t>(), dlv.as<double>(), lv.node_slot.as<int32_t>(), lv.g.slots,
+        M.F.as<double>());
+    GMGS_LAUNCHED(c);
+    GMGS_CUDA(cudaStreamSynchronize(c.stream));
+}
+
+void build_coarse_bc(Model& M) {
+    Ctx& c = M.ctx;
+    const int L = M.num_levels;
+    // restricted fixed indicator, level by level (SetupSolver.m:247-254)
+    DevBuf ind = dalloc(3 * M.levels[0].g.slots * sizeof(double));
+    k_indicator<<<blocks_for(c, M.levels[0].g.slots), 256, 0, c.stream>>>(
+        M.levels[0].g.slots, M.levels[0].nflag.as<uint8_t>(), ind.as<double>());
+    GMGS_LAUNCHED(c);
+    for (int l = 1; l < L; ++l) {
+        Level& lv = M.levels[l];
+        DevBuf indc = dalloc(3 * lv.g.slots * sizeof(double));
+        GMGS_CUDA(cudaMemsetAsync(indc.p, 0, 3 * lv.g.slots * sizeof(double), c.stream));
+        launch_restrict<double>(c, M.levels[l - 1].g, lv.g, lv.nflag.as<uint8_t>(), ind.as<double>(),
+                                indc.as<double>());
+        k_fixed_from_indicator<<<blocks_for(c, lv.g.slots), 256, 0, c.stream>>>(lv.g.slots, indc.as<double>(),
+                                                                                 lv.nflag.as<uint8_t>());
+        GMGS_LAUNCHED(c);
+        GMGS_CUDA(cudaStreamSynchronize(c.stream));
+        ind = std::move(indc);
+    }
+    // coarsest free DOFs, dense K, Cholesky, inverse
+    Level& lc = M.levels[L - 1];
+    const int64_t S = lc.g.slots;
+    DevBuf cnt = dalloc(3 * S * sizeof(int32_t));
+    k_free_count<<<blocks_for(c, 3 * S), 256, 0, c.stream>>>(S, lc.nflag.as<uint8_t>(), cnt.as<int32_t>());
+    GMGS_LAUNCHED(c);
+    const int64_t nf = exclusive_scan(c, cnt.as<int32_t>(), 3 * S);
+    if (nf == 0) throw Error(GMGS_ERR_NOT_SPD, "no free DOFs on the coarsest level");
+    if (nf > 40000) throw Error(GMGS_ERR_RESOLUTION, "coarsest level too large for a dense factorisation; use more levels");
+    M.nfree = (int)nf;
+    M.free_idx = dalloc(nf * sizeof(int32_t));
+    k_free_list<<<blocks_for(c, 3 * S), 256, 0, c.stream>>>(S, lc.nflag.as<uint8_t>(), cnt.as<int32_t>(),
+                                                             M.free_idx.as<int32_t>());
+    GMGS_LAUNCHED(c);
+    DevBuf rank = dalloc(3 * S * sizeof(int32_t));
+    k_rank_fill<<<blocks_for(c, 3 * S), 256, 0, c.stream>>>(3 * S, rank.as<int32_t>());
+    GMGS_LAUNCHED(c);
+    k_rank_set<<<blocks_for(c, nf), 256, 0, c.stream>>>(nf, M.free_idx.as<int32_t>(), rank.as<int32_t>());
+    GMGS_LAUNCHED(c);
+    M.kinv = dalloc((size_t)nf * nf * sizeof(double));
+    GMGS_CUDA(cudaMemsetAsync(M.kinv.p, 0, (size_t)nf * nf * sizeof(double), c.stream));
+    k_assemble_coarsest<<<blocks_for(c, nf * 81), 256, 0, c.stream>>>(
+        lc.g, (int)nf, M.free_idx.as<int32_t>(), rank.as<int32_t>(), lc.emask.as<uint8_t>(), lc.etype.as<int32_t>(),
+        lc.Ks64.as<double>(), M.ke0_dev.as<double>(), lc.kscale, M.kinv.as<double>());
+    GMGS_LAUNCHED(c);
+    // Kd is row-major K[row][col]; cuSOLVER is column-major, so it sees K^T.
+    // potrf/potri read the lower triangle of what they see.
+    cusolverDnHandle_t hs = nullptr;
+    if (cusolverDnCreate(&hs) != CUSOLVER_STATUS_SUCCESS) throw Error(GMGS_ERR_CUDA, "cusolverDnCreate failed");
+    struct Guard { cusolverDnHandle_t h; ~Guard() { cusolverDnDestroy(h); } } guard{hs};
+    cusolverDnSetStream(hs, c.stream);
+    int lwork = 0, lwork2 = 0;
+    const int n = (int)nf;
+    if (cusolverDnDpotrf_bufferSize(hs, CUBLAS_FILL_MODE_LOWER, n, M.kinv.as<double>(), n, &lwork) !=
+            CUSOLVER_STATUS_SUCCESS ||
+        cusolverDnDpotri_bufferSize(hs, CUBLAS_FILL_MODE_LOWER, n, M.kinv.as<double>(), n, &lwork2) !=
+            CUSOLVER_STATUS_SUCCESS)
+        throw Error(GMGS_ERR_CUDA, "cuSOLVER buffer size query failed");
+    DevBuf work = dalloc((size_t)std::max(lwork, lwork2) * sizeof(double));
+    DevBuf info = dalloc(sizeof(int));
+    if (cusolverDnDpotrf(hs, CUBLAS_FILL_MODE_LOWER, n, M.kinv.as<double>(), n, work.as<double>(), lwork,
+                         info.as<int>()) != CUSOLVER_STATUS_SUCCESS)
+        throw Error(GMGS_ERR_CUDA, "cusolverDnDpotrf failed");
+    int hinfo = 0;
+    GMGS_CUDA(cudaMemcpyAsync(&hinfo, info.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    GMGS_CUDA(cudaStreamSynchronize(c.stream));
+    if (hinfo != 0) throw Error(GMGS_ERR_NOT_SPD, "coarsest-level matrix is not positive definite");
+    if (cusolverDnDpotri(hs, CUBLAS_FILL_MODE_LOWER, n, M.kinv.as<double>(), n, work.as<double>(), lwork2,
+                         info.as<int>()) != CUSOLVER_STATUS_SUCCESS)
+        throw Error(GMGS_ERR_CUDA, "cusolverDnDpotri failed");
+    GMGS_CUDA(cudaMemcpyAsync(&hinfo, info.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    GMGS_CUDA(cudaStreamSynchronize(c.stream));
+    if (hinfo != 0) throw Error(GMGS_ERR_NOT_SPD, "coarsest-level inverse failed");
+    k_symmetrize_lower<<<blocks_for(c, (int64_t)n * n), 256, 0, c.stream>>>(n, M.kinv.as<double>());
+    GMGS_LAUNCHED(c);
+    M.cvec_in = dalloc(nf * sizeof(double));
+    M.cvec_out = dalloc(nf * sizeof(double));
+    GMGS_CUDA(cudaStreamSynchronize(c.stream));
+}
+
+}  // namespace gmgs

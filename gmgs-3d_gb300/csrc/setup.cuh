@@ -1,0 +1,67 @@
+// The state behind one gmgs_handle and the setup / solve entry points used by
+// the C ABI (api.cu).
+#pragma once
+
+#include "gmgs_internal.cuh"
+
+namespace gmgs {
+
+struct Model {
+    gmgs_params prm{};
+    int nely = 0, nelx = 0, nelz = 0;   // unpadded voxel grid
+    int ny = 0, nx = 0, nz = 0;         // padded finest grid
+    double ele[3] = {1, 1, 1};
+    int num_levels = 0;
+    bool has_density = false;
+    double penal = 3.0;
+    std::vector<Level> levels;
+    Ctx ctx;
+    bool own_stream = false;
+    double ke0_rows[KE];   // Ke0 with row = output DOF
+    DevBuf ke0_dev;
+    DevBuf rho;            // compact density (double), extension
+    // boundary conditions and solution (finest level, FP64, 3 planes)
+    DevBuf F, U;
+    double normF = 0;
+    // coarsest level
+    int nfree = 0;
+    DevBuf free_idx, kinv, cvec_in, cvec_out;
+    // outer CG work vectors
+    DevBuf cg_x, cg_r, cg_p, cg_dx, cg_q64, cg_y64, cg_z64;   // FP64 path
+    DevBuf cg_q32, cg_y32, cg_z32, cg_r32;                     // mixed path
+    DevBuf scal;           // device scalars (see solver.cu)
+    DevBuf dot_partials, dot_ticket;
+    double* scal_host = nullptr;   // pinned
+    int dot_blocks = 0;
+    bool bc_set = false, coarse_ready = false, solved = false, ops_ready = false;
+    // diagnostics
+    double t_create_ms = 0, t_bc_ms = 0, t_solve_ms = 0, t_stress_ms = 0;
+    int last_iters = 0;
+    double last_relres = 0;
+    std::string err;
+};
+
+DevBuf dalloc(size_t bytes);
+int64_t exclusive_scan(Ctx& c, int32_t* d, int64_t n);
+
+void element_stiffness(double E, double nu, const double ele[3], double Ke[KE]);
+void stress_matrices(double E, double nu, const double ele[3], double Mn[48 * 24], double Mg[48 * 24]);
+
+// setup.cu
+void build_levels(Model& M, const int32_t* occ_dev);
+void build_operators(Model& M);
+void apply_bc(Model& M, const int32_t* fixed, int64_t nfixed, const double* loads, int64_t nload);
+void build_coarse_bc(Model& M);
+void set_density_dev(Model& M, const double* rho_dev);
+
+// solver.cu
+void alloc_work(Model& M);
+int pcg_solve(Model& M, const double* b_dense, double* x_dense, int32_t* iters, double* relres, double* hist);
+void vcycle_apply_fp64(Model& M, const double* r_dense, double* z_dense);
+void apply_operator_dense(Model& M, int level, const double* x_dense, double* y_dense);
+
+// post.cu
+void stress_dev(Model& M, const double* U_dense, double* nodal_compact, float* per_voxel_compact);
+void grad_dev(Model& M, const double* U_dense, const double* lam_dense, double* dJdrho_compact);
+
+}  // namespace gmgs

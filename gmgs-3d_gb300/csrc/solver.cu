@@ -1,0 +1,213 @@
+// V-cycle preconditioner and the outer PCG (src/kernel/Vcycle.m:1-36,
+// src/kernel/CG_solver.m:1-56, src/kernel/JacobiSmoother.m:1-10).
+//
+// The FP64 path runs every vector and operator in double precision.  The
+// mixed path keeps x, r, p, the dot products and the coarsest solve in FP64
+// and runs the V-cycle (smoothers, transfers, level matvecs) in FP32; the
+// CG's own matvecs read FP64 vectors and compute in FP32.
+#include <chrono>
+#include <cmath>
+
+#include "setup.cuh"
+
+namespace gmgs {
+
+enum { SC_RZ0 = 0, SC_RZ1 = 1, SC_PQ = 2, SC_RR = 3, SC_BB = 4, SC_N = 8 };
+
+static void zalloc(Ctx& c, DevBuf& b, size_t bytes) {
+    if (b.bytes < bytes) b = dalloc(bytes);
+    GMGS_CUDA(cudaMemsetAsync(b.p, 0, bytes, c.stream));
+}
+
+void alloc_work(Model& M) {
+    Ctx& c = M.ctx;
+    const bool mixed = M.prm.precision == GMGS_MIXED;
+    const size_t T = mixed ? sizeof(float) : sizeof(double);
+    for (int l = 0; l < M.num_levels; ++l) {
+        Level& lv = M.levels[l];
+        const size_t n3 = 3 * (size_t)lv.g.slots;
+        if (l > 0) zalloc(c, lv.vr, n3 * T);
+        zalloc(c, lv.vx, n3 * T);
+        if (l < M.num_levels - 1) {
+            zalloc(c, lv.vrp, n3 * T);
+            zalloc(c, lv.vdx, n3 * T);
+            zalloc(c, lv.vy, n3 * T);
+        }
+    }
+    const size_t n3 = 3 * (size_t)M.levels[0].g.slots;
+    zalloc(c, M.cg_x, n3 * 8);
+    zalloc(c, M.cg_r, n3 * 8);
+    zalloc(c, M.cg_p, n3 * 8);
+    zalloc(c, M.cg_dx, n3 * 8);
+    if (mixed) {
+        zalloc(c, M.cg_q32, n3 * 4);
+        zalloc(c, M.cg_y32, n3 * 4);
+        zalloc(c, M.cg_z32, n3 * 4);
+        zalloc(c, M.cg_r32, n3 * 4);
+    } else {
+        zalloc(c, M.cg_q64, n3 * 8);
+        zalloc(c, M.cg_y64, n3 * 8);
+        zalloc(c, M.cg_z64, n3 * 8);
+    }
+    zalloc(c, M.scal, SC_N * sizeof(double));
+    M.dot_blocks = M.ctx.num_sms * 4;
+    zalloc(c, M.dot_partials, M.dot_blocks * sizeof(double));
+    zalloc(c, M.dot_ticket, sizeof(unsigned int));
+    if (!M.scal_host) GMGS_CUDA(cudaMallocHost(&M.scal_host, SC_N * sizeof(double)));
+    GMGS_CUDA(cudaStreamSynchronize(c.stream));
+}
+
+static DotScratch dots(Model& M) {
+    return DotScratch{M.dot_partials.as<double>(), M.dot_ticket.as<unsigned int>(), M.dot_blocks};
+}
+
+// One V(1,1) cycle, Vcycle.m:1-36: down-sweep Jacobi with residual update and
+// restriction, coarsest direct solve, up-sweep prolongation + Jacobi with the
+// pre-smoothing residual, fixed DOFs of the finest level zeroed.
+template <typename T>
+static void vcycle(Model& M, const T* r0, T* z) {
+    Ctx& c = M.ctx;
+    const int L = M.num_levels;
+    const double om = M.prm.omega;
+    for (int l = 0; l < L - 1; ++l) {
+        Level& lv = M.levels[l];
+        Level& lc = M.levels[l + 1];
+        const T* r = l == 0 ? r0 : lv.vr.as<T>();
+        const LevelView<T> v = view<T>(lv, om);
+        const int64_t n3 = 3 * lv.g.slots;
+        launch_jacobi_dx<T, T, T>(c, lv.g, v.diag, om, r, lv.vdx.as<T>());
+        launch_matvec<T, T, T>(c, v, lv.vdx.as<T>(), lv.vy.as<T>(), lv.kscale);
+        launch_diff<T>(c, n3, lv.vrp.as<T>(), r, lv.vy.as<T>());
+        launch_restrict<T>(c, lv.g, lc.g, lc.nflag.as<uint8_t>(), lv.vrp.as<T>(), lc.vr.as<T>());
+    }
+    Level& lc = M.levels[L - 1];
+    launch_gather<T>(c, M.nfree, M.free_idx.as<int32_t>(), lc.vr.as<T>(), M.cvec_in.as<double>());
+    launch_gemv(c, M.nfree, M.kinv.as<double>(), M.cvec_in.as<double>(), M.cvec_out.as<double>());
+    launch_scatter<T>(c, M.nfree, M.free_idx.as<int32_t>(), M.cvec_out.as<double>(), lc.vx.as<T>());
+    for (int l = L - 2; l >= 0; --l) {
+        Level& lv = M.levels[l];
+        T* out = l == 0 ? z : lv.vx.as<T>();
+        const LevelView<T> v = view<T>(lv, om);
+        launch_prolong_post<T>(c, lv.g, M.levels[l + 1].g, lv.nflag.as<uint8_t>(), v.diag, om,
+                               M.levels[l + 1].vx.as<T>(), lv.vdx.as<T>(), lv.vrp.as<T>(), out, l == 0);
+    }
+}
+
+void vcycle_apply(Model& M, const double* r, double* z) {
+    const int64_t n3 = 3 * M.levels[0].g.slots;
+    if (M.prm.precision == GMGS_MIXED) {
+        launch_copy<float, double>(M.ctx, n3, M.cg_r32.as<float>(), r);
+        vcycle<float>(M, M.cg_r32.as<float>(), M.cg_z32.as<float>());
+        launch_copy<double, float>(M.ctx, n3, z, M.cg_z32.as<float>());
+    } else {
+        vcycle<double>(M, r, z);
+    }
+}
+
+void vcycle_apply_fp64(Model& M, const double* r, double* z) { vcycle_apply(M, r, z); }
+
+void apply_operator_dense(Model& M, int level, const double* x, double* y) {
+    Level& lv = M.levels[level];
+    launch_matvec<double, double, double>(M.ctx, view<double>(lv, M.prm.omega), x, y, lv.kscale);
+}
+
+// CG_solver.m:1-56 with the Jacobi step before each preconditioner call.
+int pcg_solve(Model& M, const double* b, double* x, int32_t* iters_out, double* relres_out, double* hist) {
+    Ctx& c = M.ctx;
+    Level& l0 = M.levels[0];
+    const int64_t n3 = 3 * l0.g.slots;
+    const bool mixed = M.prm.precision == GMGS_MIXED;
+    const double om = M.prm.omega;
+    double* scal = M.scal.as<double>();
+    const DotScratch ds = dots(M);
+    double* r = M.cg_r.as<double>();
+    double* p = M.cg_p.as<double>();
+    double* dx = M.cg_dx.as<double>();
+    const LevelView<double> v64 = view<double>(l0, om);
+
+    launch_dot<double, double>(c, ds, n3, b, b, scal + SC_BB);
+    GMGS_CUDA(cudaMemcpyAsync(M.scal_host + SC_BB, scal + SC_BB, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    GMGS_CUDA(cudaMemsetAsync(x, 0, n3 * sizeof(double), c.stream));
+    GMGS_CUDA(cudaMemcpyAsync(r, b, n3 * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));  // r = b - A*0
+    GMGS_CUDA(cudaStreamSynchronize(c.stream));
+    const double normB = std::sqrt(M.scal_host[SC_BB]);
+    if (normB == 0.0) {
+        // zero load: the reference would divide 0/0; the solution is zero
+        if (iters_out) *iters_out = 0;
+        if (relres_out) *relres_out = 0;
+        M.last_iters = 0;
+        M.last_relres = 0;
+        return GMGS_OK;
+    }
+    if (!std::isfinite(normB)) throw Error(GMGS_ERR_NONFINITE, "non-finite load vector");
+
+    const auto t0 = std::chrono::steady_clock::now();
+    int its = 0;
+    double resnorm = INFINITY;
+    int status = GMGS_ERR_MAX_ITERATIONS;
+    const int max_it = M.prm.max_it;
+    int nhist = 0;
+    while (its <= max_it) {
+        // [x, r1] = JacobiSmoother(var)   (CG_solver.m:18-19)
+        launch_jacobi_dx<double, double, double>(c, l0.g, l0.diag64.as<double>(), om, r, dx);
+        launch_add<double, double>(c, n3, x, dx);
+        if (mixed) {
+            launch_matvec<float, double, float>(c, view<float>(l0, om), dx, M.cg_y32.as<float>(), l0.kscale);
+            launch_sub<double, float>(c, n3, r, M.cg_y32.as<float>());
+            launch_copy<float, double>(c, n3, M.cg_r32.as<float>(), r);
+            vcycle<float>(M, M.cg_r32.as<float>(), M.cg_z32.as<float>());
+        } else {
+            launch_matvec<double, double, double>(c, v64, dx, M.cg_y64.as<double>(), l0.kscale);
+            launch_sub<double, double>(c, n3, r, M.cg_y64.as<double>());
+            vcycle<double>(M, r, M.cg_z64.as<double>());
+        }
+        ++its;
+        const int cur = its & 1;
+        if (mixed) {
+            launch_dot<double, float>(c, ds, n3, r, M.cg_z32.as<float>(), scal + cur);
+            launch_p_update<float>(c, n3, M.cg_z32.as<float>(), p, scal, cur | ((its == 1) << 1));
+            launch_matvec<float, double, float>(c, view<float>(l0, om), p, M.cg_q32.as<float>(), l0.kscale);
+            launch_dot<double, float>(c, ds, n3, p, M.cg_q32.as<float>(), scal + SC_PQ);
+            launch_xr_update<float>(c, n3, x, r, p, M.cg_q32.as<float>(), scal, cur);
+        } else {
+            launch_dot<double, double>(c, ds, n3, r, M.cg_z64.as<double>(), scal + cur);
+            launch_p_update<double>(c, n3, M.cg_z64.as<double>(), p, scal, cur | ((its == 1) << 1));
+            launch_matvec<double, double, double>(c, v64, p, M.cg_q64.as<double>(), l0.kscale);
+            launch_dot<double, double>(c, ds, n3, p, M.cg_q64.as<double>(), scal + SC_PQ);
+            launch_xr_update<double>(c, n3, x, r, p, M.cg_q64.as<double>(), scal, cur);
+        }
+        launch_dot<double, double>(c, ds, n3, r, r, scal + SC_RR);
+        GMGS_CUDA(cudaMemcpyAsync(M.scal_host + SC_RR, scal + SC_RR, sizeof(double), cudaMemcpyDeviceToHost,
+                                  c.stream));
+        GMGS_CUDA(cudaStreamSynchronize(c.stream));
+        resnorm = std::sqrt(M.scal_host[SC_RR]) / normB;
+        if (M.prm.verbose) std::printf(" It.: %4d Res.: %16.6e\n", its, resnorm);
+        if (!std::isfinite(resnorm)) {
+            status = GMGS_ERR_NONFINITE;
+            break;
+        }
+        if (resnorm < M.prm.tol) {
+            status = GMGS_OK;
+            if (M.prm.verbose)
+                std::printf("CG solver converged at iteration%5d to a solution with relative residual%16.6e\n", its,
+                            resnorm);
+            break;
+        }
+        if (hist) {
+            const double t = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            hist[3 * nhist + 0] = its;
+            hist[3 * nhist + 1] = t;
+            hist[3 * nhist + 2] = resnorm;
+        }
+        ++nhist;
+    }
+    if (status == GMGS_ERR_MAX_ITERATIONS && M.prm.verbose)
+        std::printf("Exceed the maximum iterate numbers\n");
+    if (iters_out) *iters_out = its;
+    if (relres_out) *relres_out = resnorm;
+    M.last_iters = its;
+    M.last_relres = resnorm;
+    return status;
+}
+
+}  // namespace gmgs

@@ -1,0 +1,265 @@
+"""Python host side of libgmgs: a handle wrapper and a session object that
+mirrors the reference's call surface.
+
+The reference drives its solve through MATLAB globals and two functions
+(src/GMGS3D.m:11-34, src/Demo.m:67-81):
+
+    voxelizedVolume_ = CreateVoxilizedModel(...); DiscretizeDesignDomain();
+    fixingCond_ = ...; loadingCond_ = ...;
+    GetDeformation();       % -> U_
+    GetCartesianStress();   % -> cartesianStressField_
+
+`Session` keeps the same names (tol_, maxIT_, weightFactorJacobi_, moduls_,
+poissonRatio_, coarsestResolutionControl_, voxelizedVolume_, fixingCond_,
+loadingCond_, U_, cartesianStressField_, iterationHist_) and methods
+(DiscretizeDesignDomain, GetDeformation, GetCartesianStress).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+
+
+class GMGSError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"[{status}] {message}")
+        self.status = status
+
+
+def _dptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double)) if a is not None else None
+
+
+def _fptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float)) if a is not None else None
+
+
+def _iptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+class Solver:
+    """One gmgs_handle: model + hierarchy on the current CUDA device."""
+
+    def __init__(self, voxels, *, ele_size=(1.0, 1.0, 1.0), tol=1e-3, max_it=20000, omega=0.4,
+                 youngs_modulus=1.0, poisson_ratio=0.3, coarsest_resolution_control=10000,
+                 num_levels=0, precision="fp64", verbose=False):
+        self._lib = L.load()
+        vox = np.asfortranarray(np.asarray(voxels, dtype=np.int32))
+        if vox.ndim != 3:
+            raise ValueError("voxels must be a (ny, nx, nz) array")
+        self.shape = vox.shape
+        p = L.Params()
+        self._lib.gmgs_default_params(C.byref(p))
+        p.tol = tol
+        p.max_it = max_it
+        p.omega = omega
+        p.youngs_modulus = youngs_modulus
+        p.poisson_ratio = poisson_ratio
+        p.coarsest_resolution_control = coarsest_resolution_control
+        p.num_levels = num_levels
+        p.precision = {"fp64": L.FP64, "mixed": L.MIXED}[precision] if isinstance(precision, str) else int(precision)
+        p.verbose = int(bool(verbose))
+        self.params = p
+        flat = np.ascontiguousarray(vox.ravel(order="F"))
+        es = np.asarray(ele_size, dtype=np.float64)
+        h = C.c_void_p()
+        st = self._lib.gmgs_create(_iptr(flat), vox.shape[0], vox.shape[1], vox.shape[2], _dptr(es),
+                                   C.byref(p), C.byref(h))
+        if st != L.OK:
+            raise GMGSError(st, self._lib.gmgs_last_error(None).decode())
+        self._h = h
+        self.iterations = 0
+        self.relres = float("nan")
+        self.status = L.OK
+
+    # ------------------------------------------------------------------ utils
+    def _check(self, st, allow=()):
+        if st != L.OK and st not in allow:
+            raise GMGSError(st, self._lib.gmgs_last_error(self._h).decode())
+        return st
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.gmgs_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def num_levels(self) -> int:
+        v = C.c_int32()
+        self._check(self._lib.gmgs_num_levels(self._h, C.byref(v)))
+        return v.value
+
+    def num_nodes(self, level: int = 1) -> int:
+        v = C.c_int64()
+        self._check(self._lib.gmgs_num_nodes(self._h, level, C.byref(v)))
+        return v.value
+
+    def num_elements(self, level: int = 1) -> int:
+        v = C.c_int64()
+        self._check(self._lib.gmgs_num_elements(self._h, level, C.byref(v)))
+        return v.value
+
+    @property
+    def padded_dims(self):
+        d = (C.c_int32 * 3)()
+        self._check(self._lib.gmgs_padded_dims(self._h, d))
+        return tuple(d)
+
+    @property
+    def device_bytes(self) -> int:
+        v = C.c_int64()
+        self._check(self._lib.gmgs_device_bytes(self._h, C.byref(v)))
+        return v.value
+
+    @property
+    def launch_count(self) -> int:
+        v = C.c_int64()
+        self._check(self._lib.gmgs_launch_count(self._h, C.byref(v)))
+        return v.value
+
+    @property
+    def phase_times_ms(self):
+        d = (C.c_double * 4)()
+        self._check(self._lib.gmgs_phase_times(self._h, d))
+        return {"create": d[0], "bc_setup": d[1], "solve": d[2], "stress": d[3]}
+
+    def set_stream(self, stream_ptr: int | None):
+        self._check(self._lib.gmgs_set_stream(self._h, C.c_void_p(stream_ptr or 0)))
+
+    def set_tolerance(self, tol: float, max_it: int):
+        self._check(self._lib.gmgs_set_tolerance(self._h, tol, max_it))
+
+    # ---------------------------------------------------------------- the path
+    def set_bc(self, fixed_nodes, loads):
+        fixed = np.ascontiguousarray(np.asarray(fixed_nodes).ravel(), dtype=np.int32)
+        ld = np.ascontiguousarray(np.asarray(loads, dtype=np.float64).reshape(-1, 4))
+        self._check(self._lib.gmgs_set_bc(self._h, _iptr(fixed) if fixed.size else None, fixed.size,
+                                          _dptr(ld) if ld.size else None, ld.shape[0]))
+
+    def set_density(self, rho, penal: float = 3.0):
+        r = np.ascontiguousarray(np.asarray(rho, dtype=np.float64).ravel())
+        if r.size != self.num_elements(1):
+            raise ValueError("rho must have one entry per solid voxel")
+        self._check(self._lib.gmgs_set_density(self._h, _dptr(r), penal))
+
+    def solve(self, with_history=False):
+        """Return U (3*num_nodes, interleaved); raise on divergence."""
+        nn = self.num_nodes(1)
+        U = np.empty(3 * nn)
+        it = C.c_int32()
+        rr = C.c_double()
+        hist = np.zeros(3 * (self.params.max_it + 2)) if with_history else None
+        st = self._check(self._lib.gmgs_solve(self._h, _dptr(U), C.byref(it), C.byref(rr), _dptr(hist)),
+                         allow=(L.ERR_MAX_ITERATIONS,))
+        self.status, self.iterations, self.relres = st, it.value, rr.value
+        if with_history:
+            nrows = self.iterations - 1 if st == L.OK else self.iterations
+            self.history = hist[:3 * max(nrows, 0)].reshape(-1, 3)
+        return U
+
+    def solve_dev(self, U_dev_ptr: int | None):
+        it = C.c_int32()
+        rr = C.c_double()
+        st = self._check(self._lib.gmgs_solve_dev(self._h, C.c_void_p(U_dev_ptr or 0), C.byref(it), C.byref(rr), None),
+                         allow=(L.ERR_MAX_ITERATIONS,))
+        self.status, self.iterations, self.relres = st, it.value, rr.value
+        return st
+
+    def stress(self, per_voxel=True):
+        nodal = np.empty((self.num_nodes(1), 6))
+        vox = np.empty((self.num_elements(1), 6), dtype=np.float32) if per_voxel else None
+        self._check(self._lib.gmgs_stress(self._h, _dptr(nodal), _fptr(vox)))
+        return (nodal, vox) if per_voxel else nodal
+
+    def grad(self, ell=None):
+        out = np.empty(self.num_elements(1))
+        e = None if ell is None else np.ascontiguousarray(np.asarray(ell, dtype=np.float64).ravel())
+        self._check(self._lib.gmgs_grad(self._h, _dptr(e), _dptr(out)))
+        return out
+
+    def apply_operator(self, x, level: int = 1):
+        """AtX(x, level) on compact interleaved vectors."""
+        x = np.ascontiguousarray(np.asarray(x, dtype=np.float64))
+        y = np.empty_like(x)
+        self._check(self._lib.gmgs_apply_operator(self._h, level, _dptr(x), _dptr(y)))
+        return y
+
+    def apply_preconditioner(self, r):
+        """Vcycle(r) on a compact interleaved finest-level vector."""
+        r = np.ascontiguousarray(np.asarray(r, dtype=np.float64))
+        z = np.empty_like(r)
+        self._check(self._lib.gmgs_apply_preconditioner(self._h, _dptr(r), _dptr(z)))
+        return z
+
+
+class Session:
+    """The reference's global workspace and entry points (src/GlobalVariables.m:3-38)."""
+
+    def __init__(self):
+        self.tol_ = 1.0e-3
+        self.maxIT_ = 20000
+        self.weightFactorJacobi_ = 0.4
+        self.moduls_ = 1.0
+        self.poissonRatio_ = 0.3
+        self.coarsestResolutionControl_ = 10000
+        self.numLevels_ = 0            # 0 = the reference's rule
+        self.eleSize_ = (1.0, 1.0, 1.0)
+        self.precision_ = "fp64"
+        self.voxelizedVolume_ = None
+        self.fixingCond_ = None
+        self.loadingCond_ = None
+        self.F_ = None
+        self.U_ = None
+        self.cartesianStressField_ = None
+        self.iterationHist_ = np.zeros((0, 3))
+        self._solver = None
+
+    def CreateVoxilizedModel(self, nx, ny, nz):
+        """Solid cuboid overload (src/common/CreateVoxilizedModel.m:27-32)."""
+        self.voxelizedVolume_ = np.ones((ny, nx, nz), dtype=np.int32)
+        return self.voxelizedVolume_
+
+    def DiscretizeDesignDomain(self):
+        self._solver = Solver(self.voxelizedVolume_, ele_size=self.eleSize_, tol=self.tol_, max_it=self.maxIT_,
+                              omega=self.weightFactorJacobi_, youngs_modulus=self.moduls_,
+                              poisson_ratio=self.poissonRatio_,
+                              coarsest_resolution_control=self.coarsestResolutionControl_,
+                              num_levels=self.numLevels_, precision=self.precision_)
+        return self._solver
+
+    @property
+    def numLevels(self):
+        return self._solver.num_levels
+
+    def GetDeformation(self):
+        if self._solver is None:
+            self.DiscretizeDesignDomain()
+        self._solver.set_bc(self.fixingCond_, self.loadingCond_)
+        self._solver.set_tolerance(self.tol_, self.maxIT_)
+        self.U_ = self._solver.solve(with_history=True)
+        self.iterationHist_ = np.vstack([self.iterationHist_, self._solver.history])
+        return self.U_
+
+    def GetCartesianStress(self):
+        self.cartesianStressField_ = self._solver.stress(per_voxel=False)
+        return self.cartesianStressField_

@@ -1,0 +1,127 @@
+"""Parity of the CUDA path (through the C ABI) with the CPU oracle.
+
+FP64 path: operators and V-cycle to 1e-11 relative, PCG iteration counts
+identical, residual histories to 1e-8 relative, displacement to 1e-6
+relative (the displacement bar of the drop-in), stress to 1e-8 relative.
+Mixed path: same iteration count or one off, displacement within 1e-4
+relative of the FP64 oracle solve at tolerance 1e-3.
+"""
+import numpy as np
+import pytest
+
+from gmgs import Solver, synthetic
+from gmgs_oracle import Oracle, Params
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return np.linalg.norm(np.asarray(a) - np.asarray(b)) / max(np.linalg.norm(np.asarray(b)), 1e-300)
+
+
+CASES = {
+    # name: (voxels builder, num_levels, omega)
+    "cube12_L3": (lambda: np.ones((12, 12, 12), np.int32), 3, 0.4),
+    "block42_L4": (lambda: synthetic.make("block42_fp64")[0], 4, 0.4),
+    "ragged_L3": (lambda: synthetic.sphere_voids(21, 13, 18, 6, 7), 3, 0.4),
+}
+
+
+def _pair(name, precision="fp64", tol=1e-3):
+    build, L, omega = CASES[name]
+    vox = build()
+    fixed, loads = synthetic.boundary_conditions(vox, L)
+    o = Oracle(vox, Params(omega=omega, num_levels=L, tol=tol))
+    o.apply_boundary_condition(fixed, loads)
+    s = Solver(vox, omega=omega, num_levels=L, tol=tol, precision=precision)
+    s.set_bc(fixed, loads)
+    return o, s
+
+
+@pytest.fixture(scope="module", params=list(CASES))
+def solved_pair(request):
+    o, s = _pair(request.param)
+    u_ref = o.get_deformation()
+    u = s.solve(with_history=True)
+    return request.param, o, s, u_ref, u
+
+
+def test_sizes_match(solved_pair):
+    _, o, s, _, _ = solved_pair
+    assert s.num_levels == o.numLevels
+    for l, lv in enumerate(o.levels):
+        assert s.num_nodes(l + 1) == lv.numNodes
+        assert s.num_elements(l + 1) == lv.numElements
+
+
+def test_operator_each_level(solved_pair):
+    _, o, s, _, _ = solved_pair
+    rng = np.random.default_rng(0)
+    for l, lv in enumerate(o.levels):
+        x = rng.standard_normal(lv.numDOFs)
+        y_ref = o.atx(x, l)
+        y = s.apply_operator(x, l + 1)
+        assert rel(y, y_ref) < 1e-11, f"level {l + 1}"
+
+
+def test_vcycle(solved_pair):
+    _, o, s, _, _ = solved_pair
+    rng = np.random.default_rng(1)
+    r = rng.standard_normal(o.levels[0].numDOFs)
+    r[o.levels[0].fixedDOFs] = 0
+    assert rel(s.apply_preconditioner(r), o.vcycle(r)) < 1e-10
+
+
+def test_pcg_history_and_displacement(solved_pair):
+    _, o, s, u_ref, u = solved_pair
+    assert s.status == 0
+    assert s.iterations == o.iterations
+    h_ref = np.array([h[2] for h in o.iterationHist])
+    assert s.history.shape[0] == len(h_ref)
+    if len(h_ref):
+        assert np.max(np.abs(s.history[:, 2] - h_ref) / h_ref) < 1e-8
+    assert abs(s.relres - o.relres) / o.relres < 1e-8
+    assert rel(u, u_ref) < 1e-6
+
+
+def test_stress(solved_pair):
+    _, o, s, u_ref, u = solved_pair
+    nodal_ref, vox_ref = o.get_cartesian_stress()
+    nodal, vox = s.stress()
+    assert rel(nodal, nodal_ref) < 1e-6
+    assert rel(vox, vox_ref) < 1e-5   # FP32 output
+
+
+def test_mixed_precision_error():
+    o, s = _pair("block42_L4", precision="mixed")
+    u_ref = o.get_deformation()
+    u = s.solve()
+    assert s.status == 0
+    assert abs(s.iterations - o.iterations) <= 1
+    assert rel(u, u_ref) < 1e-4
+
+
+def test_divergent_omega_matches_oracle():
+    """omega = 0.6 diverges on void models in the reference algorithm as well:
+    both residual histories grow identically until the solve gives up."""
+    vox = synthetic.make("block42_fp64")[0]
+    fixed, loads = synthetic.boundary_conditions(vox, 4)
+    o = Oracle(vox, Params(omega=0.6, num_levels=4, max_it=12))
+    o.apply_boundary_condition(fixed, loads)
+    with np.errstate(all="ignore"):
+        o.get_deformation()
+    s = Solver(vox, omega=0.6, num_levels=4, max_it=12)
+    s.set_bc(fixed, loads)
+    s.solve(with_history=True)
+    assert s.status == 7       # GMGS_ERR_MAX_ITERATIONS
+    h_ref = np.array([h[2] for h in o.iterationHist])
+    assert len(h_ref) == 13 and s.history.shape[0] == 13
+    assert h_ref[-1] > h_ref[0]
+    assert np.max(np.abs(s.history[:, 2] - h_ref) / h_ref) < 1e-6
+
+
+def test_repeat_solve_is_bitwise_identical():
+    _, s = _pair("ragged_L3")
+    u1 = s.solve()
+    u2 = s.solve()
+    assert np.array_equal(u1, u2)

@@ -1,0 +1,332 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 GMGS-3D solve.
+
+Metric: seconds for one V-cycle-preconditioned CG solve to relative residual
+1e-3 on the 337 x 294 x 512 voxel block with 120 seeded spherical voids,
+6 multigrid levels, mixed precision (FP32 V-cycle, FP64 outer CG vectors,
+dots and coarsest solve), next to the plain FP64 GPU path and the CPU oracle.
+
+A step is one full solve from x = 0 with the model, hierarchy and boundary
+conditions resident in HBM.  The vectors (>1 GB each) are larger than L2, so
+no L2 flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gmgs|reference]
+
+Under torchrun with N > 1 every rank solves its own replica of the workload
+on its own GPU (the solve does not shard: replicas only); rank 0 prints.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+for _p in (ROOT / "gmgs-3d_gb300", ROOT / "oracle"):
+    if str(_p) not in sys.path:
+        sys.path.insert(0, str(_p))
+
+METRIC = "Solve s to rel-res 1e-3 at 52M DOF: mixed vs FP64 V-cycle; matvec GB/s vs HBM"
+WORKLOAD = "block337_mixed_L6"
+CLOCK_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gmgs", choices=["gmgs", "reference"])
+    ap.add_argument("--workload", default=WORKLOAD)
+    ap.add_argument("--scale", type=float, default=1.0, help="linear resolution scale (tests only)")
+    ap.add_argument("--omega", type=float, default=0.4)
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison solve")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle sample")
+    ap.add_argument("--cpu-scale", type=float, default=0.125)
+    return ap.parse_args()
+
+
+# --------------------------------------------------------------------------
+# clocks during the timed region
+# --------------------------------------------------------------------------
+class ClockSampler:
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={CLOCK_FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9 and parts[1].replace(".", "").isdigit():
+                    rows.append(parts)
+        except OSError:
+            pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[1]) for r in rows]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": float(rows[0][2]), "reasons": reasons,
+                "samples": len(rows), "power_w_max": max(float(r[3]) for r in rows if r[3].replace(".", "").isdigit())}
+
+
+# --------------------------------------------------------------------------
+# CPU oracle sample (the reference's algorithm restated in NumPy), in a child process
+# --------------------------------------------------------------------------
+CPU_SAMPLE = r"""
+import json, os, sys, time
+sys.path[:0] = [sys.argv[1] + '/gmgs-3d_gb300', sys.argv[1] + '/oracle']
+import numpy as np
+from gmgs import synthetic
+from gmgs_oracle import Oracle, Params
+w = synthetic.WORKLOADS[sys.argv[2]]
+scale = float(sys.argv[3]); omega = float(sys.argv[4]); iters = int(sys.argv[5])
+drop = max(0, int(round(-np.log2(scale))))
+L = max(2, (w.num_levels or 5) - drop)
+vox = synthetic.sphere_voids(max(2, round(w.nelx*scale)), max(2, round(w.nely*scale)), max(2, round(w.nelz*scale)), max(1, round(w.voids*scale**2)), w.seed)
+fixed, loads = synthetic.boundary_conditions(vox, L)
+t0 = time.perf_counter()
+o = Oracle(vox, Params(omega=omega, num_levels=L, max_it=iters - 1))
+o.apply_boundary_condition(fixed, loads)
+o.setup()
+t1 = time.perf_counter()
+with np.errstate(all='ignore'):
+    o.cg(o.F)
+t2 = time.perf_counter()
+print(json.dumps({"dofs": int(o.levels[0].numDOFs), "setup_s": t1 - t0, "iter_s": (t2 - t1) / o.iterations,
+                  "its": o.iterations, "shape": list(vox.shape), "levels": L}))
+"""
+
+
+def cpu_sample(workload: str, scale: float, omega: float, iters: int = 8) -> dict:
+    res = subprocess.run([sys.executable, "-c", CPU_SAMPLE, str(ROOT), workload, str(scale), str(omega), str(iters)],
+                         capture_output=True, text=True, timeout=900)
+    if res.returncode != 0:
+        raise RuntimeError(res.stderr[-2000:])
+    return json.loads(res.stdout.strip().splitlines()[-1])
+
+
+def cpu_extrapolate(sample: dict, dofs_full: int, its_full: int) -> float:
+    """Seconds for the full solve, scaled linearly in DOFs from the sample."""
+    ratio = dofs_full / sample["dofs"]
+    return (sample["setup_s"] + sample["iter_s"] * its_full) * ratio
+
+
+# --------------------------------------------------------------------------
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def run_reference(a):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    import numpy as np
+    from gmgs import synthetic
+    vox, fixed, loads, L, _ = synthetic.make(a.workload, scale=a.scale)
+    # DOFs of the full workload, from the node mask of the padded grid
+    nely, nelx, nelz = vox.shape
+    pad = synthetic.padded_shape(nely, nelx, nelz, L)
+    p = np.zeros(pad, np.int32)
+    p[:nely, :nelx, :nelz] = vox
+    dofs_full = 3 * int(synthetic.solid_node_mask(p).sum())
+    its_full = int(os.environ.get("GMGS_REF_ITERS", "0")) or 60
+    vals = []
+    samples = []
+    for i in range(a.warmup + a.steps):
+        s = cpu_sample(a.workload, a.cpu_scale, a.omega)
+        if i >= a.warmup:
+            samples.append(s)
+            vals.append(cpu_extrapolate(s, dofs_full, its_full))
+    v = statistics.median(vals)
+    s = samples[0]
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": a.gpus, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": a.workload, "dofs": dofs_full, "levels": L, "omega": a.omega, "tol": 1e-3},
+        "cpu_baseline": {"value": v, "unit": "s", "cores": os.cpu_count(), "kind": "port",
+                         "sample": f"NumPy oracle: setup + {s['its']} CG iterations on the same generator at "
+                                   f"{s['shape']} ({s['dofs']} DOFs, {s['levels']} levels), scaled linearly by DOFs "
+                                   f"to {dofs_full} DOFs and {its_full} iterations"},
+        "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_gmgs(a):
+    import numpy as np
+    import torch
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    from gmgs import Solver, synthetic
+
+    w = synthetic.WORKLOADS[a.workload]
+    t0 = time.perf_counter()
+    vox, fixed, loads, L, rho = synthetic.make(a.workload, scale=a.scale)
+    t_gen = time.perf_counter() - t0
+
+    stream = torch.cuda.Stream()
+    s = Solver(vox, omega=a.omega, num_levels=L, tol=w.tol, precision="mixed")
+    s.set_stream(stream.cuda_stream)
+    s.set_bc(fixed, loads)
+    nn = s.num_nodes(1)
+    dofs = 3 * nn
+
+    def timed(solver, k):
+        solver.set_profiling(True)
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(k):
+            solver.solve_dev(None)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+        return e0.elapsed_time(e1) / k
+
+    for _ in range(a.warmup):
+        s.solve_dev(None)
+    l0 = s.launch_count
+    with ClockSampler(local) as clk:
+        ms = timed(s, a.steps)
+    launches = s.launch_count - l0
+    its = s.iterations
+    relres = s.relres
+    nl, mv_ms, mv_bytes = s.kernel_time(0)
+    if ws > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+
+    out = {}
+    if rank == 0 and not a.no_fp64:
+        u_mixed = s.solve()
+        s64 = Solver(vox, omega=a.omega, num_levels=L, tol=w.tol, precision="fp64")
+        s64.set_stream(stream.cuda_stream)
+        s64.set_bc(fixed, loads)
+        ms64 = timed(s64, 1)
+        u64 = s64.solve()
+        out["fp64"] = {"seconds": ms64 / 1e3, "iterations": s64.iterations, "relres": s64.relres,
+                       "speedup_mixed_vs_fp64": ms64 / ms,
+                       "displacement_rel_err_mixed_vs_fp64": float(np.linalg.norm(u_mixed - u64) / np.linalg.norm(u64))}
+        n64, ms64_mv, b64 = s64.kernel_time(0)
+        out["fp64"]["fine_matvec_ms_per_launch"] = ms64_mv / max(n64, 1)
+        s64.close()
+
+    e2e = None
+    if rank == 0 and not a.no_e2e:
+        occ_bytes = vox.size * 4
+        bc_bytes = fixed.size * 4 + loads.size * 8
+        times = []
+        for i in range(2):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            se = Solver(vox, omega=a.omega, num_levels=L, tol=w.tol, precision="mixed")
+            se.set_bc(fixed, loads)
+            u = se.solve()
+            torch.cuda.synchronize()
+            times.append(time.perf_counter() - t0)
+            phases = se.phase_times_ms
+            se.close()
+        e2e = {"value": times[-1], "unit": "s", "h2d_bytes_per_step": int(occ_bytes + bc_bytes),
+               "d2h_bytes_per_step": int(u.nbytes), "phases_ms": phases}
+
+    cpu = None
+    if rank == 0 and not a.no_cpu:
+        smp = cpu_sample(a.workload, a.cpu_scale, a.omega)
+        v = cpu_extrapolate(smp, dofs, its)
+        cpu = {"value": v, "unit": "s", "cores": 1, "kind": "port",
+               "sample": f"NumPy oracle: setup + {smp['its']} CG iterations on the same generator at {smp['shape']} "
+                         f"({smp['dofs']} DOFs, {smp['levels']} levels) = {smp['setup_s']:.1f} s + "
+                         f"{smp['iter_s']:.2f} s/iteration, scaled linearly by DOFs to {dofs} DOFs and {its} iterations"}
+
+    if rank != 0:
+        return
+    peaks = {}
+    try:
+        peaks = json.load(open(ROOT / "MEASURED_PEAKS.json"))
+    except OSError:
+        pass
+    hbm = peaks.get("hbm_gbs")
+    peak_note = "measured" if hbm else "fallback"
+    hbm = hbm or 6800.0
+    achieved = mv_bytes / (mv_ms / 1e3) / 1e9 if mv_ms > 0 else None
+    line = {
+        "metric": METRIC, "value": ms / 1e3, "unit": "s", "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 V-cycle / f64 CG", "data": "synthetic",
+        "config": {"workload": a.workload, "resolution": [w.nelx, w.nely, w.nelz], "voids": w.voids,
+                   "levels": L, "padded": list(s.padded_dims), "dofs": dofs, "omega": a.omega, "tol": w.tol,
+                   "iterations": its, "relres": relres, "l2": "inputs larger than L2 (no flush)",
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "dof_iterations_per_s": dofs * its / (ms / 1e3),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm if achieved else None, "traffic": None,
+                     "kernel": "finest-level K*x", "launches_timed": nl,
+                     "ms_per_launch": mv_ms / max(nl, 1), "peak_source": peak_note},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "device_bytes": s.device_bytes,
+        "generate_s": t_gen,
+    }
+    line.update(out)
+    print(json.dumps(line))
+    s.close()
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_gmgs(a)
+
+
+if __name__ == "__main__":
+    main()

@@ -456,11 +456,43 @@ int gmgs_phase_times(const gmgs_handle* h, double out[4]) {
     return GMGS_OK;
 }
 
+int gmgs_set_profiling(gmgs_handle* h, int32_t enable) {
+    return guarded(h, [&]() -> int {
+        if (!h) fail(GMGS_ERR_INVALID_ARGUMENT, "handle is NULL");
+        gmgs::Ctx& c = h->M.ctx;
+        GMGS_CUDA(cudaStreamSynchronize(c.stream));
+        for (auto& s : c.prof_slot) { s.used = 0; s.bytes = 0; }
+        c.prof = enable != 0;
+        return GMGS_OK;
+    });
+}
+
+int gmgs_kernel_time(gmgs_handle* h, int32_t kernel, int64_t* launches, double* total_ms, double* bytes) {
+    return guarded(h, [&]() -> int {
+        if (!h || kernel < 0 || kernel >= gmgs::PK_COUNT) fail(GMGS_ERR_INVALID_ARGUMENT, "bad kernel id");
+        gmgs::Ctx& c = h->M.ctx;
+        GMGS_CUDA(cudaStreamSynchronize(c.stream));
+        const gmgs::ProfSlot& s = c.prof_slot[kernel];
+        double tot = 0;
+        for (int i = 0; i + 1 < s.used; i += 2) {
+            float ms = 0;
+            GMGS_CUDA(cudaEventElapsedTime(&ms, s.ev[i], s.ev[i + 1]));
+            tot += ms;
+        }
+        if (launches) *launches = s.used / 2;
+        if (total_ms) *total_ms = tot;
+        if (bytes) *bytes = s.bytes;
+        return GMGS_OK;
+    });
+}
+
 void gmgs_destroy(gmgs_handle* h) {
     if (!h) return;
     gmgs::Model& M = h->M;
     if (M.ctx.stream) cudaStreamSynchronize(M.ctx.stream);
     M.levels.clear();
+    for (auto& s : M.ctx.prof_slot)
+        for (cudaEvent_t e : s.ev) cudaEventDestroy(e);
     if (M.scal_host) cudaFreeHost(M.scal_host);
     const bool own = M.own_stream;
     cudaStream_t s = M.ctx.stream;

@@ -140,10 +140,33 @@ struct Level {
     DevBuf vr, vrp, vdx, vx, vy;
 };
 
+// Per-launch CUDA-event timing of selected kernels (diagnostics; off by default).
+enum ProfKernel { PK_FINE_MATVEC = 0, PK_VCYCLE = 1, PK_CG_ITER = 2, PK_COUNT = 3 };
+
+struct ProfSlot {
+    std::vector<cudaEvent_t> ev;   // start/stop pairs
+    int used = 0;                  // events in use (2 per launch)
+    double bytes = 0;              // algorithmic bytes of the recorded launches
+};
+
 struct Ctx {
     cudaStream_t stream = nullptr;
     int64_t launches = 0;
     int num_sms = 148;
+    bool prof = false;
+    ProfSlot prof_slot[PK_COUNT];
+    // record a start (stop=false) or stop event for kernel k
+    void mark(int k, bool stop, double bytes = 0) {
+        if (!prof) return;
+        ProfSlot& s = prof_slot[k];
+        if ((int)s.ev.size() <= s.used) {
+            cudaEvent_t e;
+            if (cudaEventCreate(&e) != cudaSuccess) return;
+            s.ev.push_back(e);
+        }
+        cudaEventRecord(s.ev[s.used++], stream);
+        if (stop) s.bytes += bytes;
+    }
 };
 
 // ---------------------------------------------------------------------------

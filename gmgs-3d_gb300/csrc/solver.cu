@@ -57,6 +57,17 @@ void alloc_work(Model& M) {
     GMGS_CUDA(cudaStreamSynchronize(c.stream));
 }
 
+// level-0 matvec with optional event timing; algorithmic bytes: read x and
+// write y at every solid node, one mask byte per solid element and node
+template <typename Tc, typename Tin, typename Tout>
+static void fine_matvec(Model& M, const Tin* x, Tout* y) {
+    Level& l0 = M.levels[0];
+    const double bytes = (double)l0.n_node * (3.0 * sizeof(Tin) + 3.0 * sizeof(Tout) + 1.0) + (double)l0.n_elem;
+    M.ctx.mark(PK_FINE_MATVEC, false);
+    launch_matvec<Tc, Tin, Tout>(M.ctx, view<Tc>(l0, M.prm.omega), x, y, l0.kscale);
+    M.ctx.mark(PK_FINE_MATVEC, true, bytes);
+}
+
 static DotScratch dots(Model& M) {
     return DotScratch{M.dot_partials.as<double>(), M.dot_ticket.as<unsigned int>(), M.dot_blocks};
 }
@@ -67,6 +78,7 @@ static DotScratch dots(Model& M) {
 template <typename T>
 static void vcycle(Model& M, const T* r0, T* z) {
     Ctx& c = M.ctx;
+    c.mark(PK_VCYCLE, false);
     const int L = M.num_levels;
     const double om = M.prm.omega;
     for (int l = 0; l < L - 1; ++l) {
@@ -76,7 +88,8 @@ static void vcycle(Model& M, const T* r0, T* z) {
         const LevelView<T> v = view<T>(lv, om);
         const int64_t n3 = 3 * lv.g.slots;
         launch_jacobi_dx<T, T, T>(c, lv.g, v.diag, om, r, lv.vdx.as<T>());
-        launch_matvec<T, T, T>(c, v, lv.vdx.as<T>(), lv.vy.as<T>(), lv.kscale);
+        if (l == 0) fine_matvec<T, T, T>(M, lv.vdx.as<T>(), lv.vy.as<T>());
+        else launch_matvec<T, T, T>(c, v, lv.vdx.as<T>(), lv.vy.as<T>(), lv.kscale);
         launch_diff<T>(c, n3, lv.vrp.as<T>(), r, lv.vy.as<T>());
         launch_restrict<T>(c, lv.g, lc.g, lc.nflag.as<uint8_t>(), lv.vrp.as<T>(), lc.vr.as<T>());
     }
@@ -91,6 +104,7 @@ static void vcycle(Model& M, const T* r0, T* z) {
         launch_prolong_post<T>(c, lv.g, M.levels[l + 1].g, lv.nflag.as<uint8_t>(), v.diag, om,
                                M.levels[l + 1].vx.as<T>(), lv.vdx.as<T>(), lv.vrp.as<T>(), out, l == 0);
     }
+    c.mark(PK_VCYCLE, true);
 }
 
 void vcycle_apply(Model& M, const double* r, double* z) {
@@ -123,7 +137,6 @@ int pcg_solve(Model& M, const double* b, double* x, int32_t* iters_out, double* 
     double* r = M.cg_r.as<double>();
     double* p = M.cg_p.as<double>();
     double* dx = M.cg_dx.as<double>();
-    const LevelView<double> v64 = view<double>(l0, om);
 
     launch_dot<double, double>(c, ds, n3, b, b, scal + SC_BB);
     GMGS_CUDA(cudaMemcpyAsync(M.scal_host + SC_BB, scal + SC_BB, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
@@ -148,16 +161,17 @@ int pcg_solve(Model& M, const double* b, double* x, int32_t* iters_out, double* 
     const int max_it = M.prm.max_it;
     int nhist = 0;
     while (its <= max_it) {
+        c.mark(PK_CG_ITER, false);
         // [x, r1] = JacobiSmoother(var)   (CG_solver.m:18-19)
         launch_jacobi_dx<double, double, double>(c, l0.g, l0.diag64.as<double>(), om, r, dx);
         launch_add<double, double>(c, n3, x, dx);
         if (mixed) {
-            launch_matvec<float, double, float>(c, view<float>(l0, om), dx, M.cg_y32.as<float>(), l0.kscale);
+            fine_matvec<float, double, float>(M, dx, M.cg_y32.as<float>());
             launch_sub<double, float>(c, n3, r, M.cg_y32.as<float>());
             launch_copy<float, double>(c, n3, M.cg_r32.as<float>(), r);
             vcycle<float>(M, M.cg_r32.as<float>(), M.cg_z32.as<float>());
         } else {
-            launch_matvec<double, double, double>(c, v64, dx, M.cg_y64.as<double>(), l0.kscale);
+            fine_matvec<double, double, double>(M, dx, M.cg_y64.as<double>());
             launch_sub<double, double>(c, n3, r, M.cg_y64.as<double>());
             vcycle<double>(M, r, M.cg_z64.as<double>());
         }
@@ -166,17 +180,18 @@ int pcg_solve(Model& M, const double* b, double* x, int32_t* iters_out, double* 
         if (mixed) {
             launch_dot<double, float>(c, ds, n3, r, M.cg_z32.as<float>(), scal + cur);
             launch_p_update<float>(c, n3, M.cg_z32.as<float>(), p, scal, cur | ((its == 1) << 1));
-            launch_matvec<float, double, float>(c, view<float>(l0, om), p, M.cg_q32.as<float>(), l0.kscale);
+            fine_matvec<float, double, float>(M, p, M.cg_q32.as<float>());
             launch_dot<double, float>(c, ds, n3, p, M.cg_q32.as<float>(), scal + SC_PQ);
             launch_xr_update<float>(c, n3, x, r, p, M.cg_q32.as<float>(), scal, cur);
         } else {
             launch_dot<double, double>(c, ds, n3, r, M.cg_z64.as<double>(), scal + cur);
             launch_p_update<double>(c, n3, M.cg_z64.as<double>(), p, scal, cur | ((its == 1) << 1));
-            launch_matvec<double, double, double>(c, v64, p, M.cg_q64.as<double>(), l0.kscale);
+            fine_matvec<double, double, double>(M, p, M.cg_q64.as<double>());
             launch_dot<double, double>(c, ds, n3, p, M.cg_q64.as<double>(), scal + SC_PQ);
             launch_xr_update<double>(c, n3, x, r, p, M.cg_q64.as<double>(), scal, cur);
         }
         launch_dot<double, double>(c, ds, n3, r, r, scal + SC_RR);
+        c.mark(PK_CG_ITER, true);
         GMGS_CUDA(cudaMemcpyAsync(M.scal_host + SC_RR, scal + SC_RR, sizeof(double), cudaMemcpyDeviceToHost,
                                   c.stream));
         GMGS_CUDA(cudaStreamSynchronize(c.stream));

@@ -69,6 +69,8 @@ SIGNATURES = {
     "gmgs_device_bytes": (C.c_int, [_p, _i64p]),
     "gmgs_launch_count": (C.c_int, [_p, _i64p]),
     "gmgs_phase_times": (C.c_int, [_p, _dp]),
+    "gmgs_set_profiling": (C.c_int, [_p, _i32]),
+    "gmgs_kernel_time": (C.c_int, [_p, _i32, _i64p, _dp, _dp]),
     "gmgs_last_error": (C.c_char_p, [_p]),
     "gmgs_status_string": (C.c_char_p, [C.c_int]),
     "gmgs_destroy": (None, [_p]),

@@ -143,6 +143,17 @@ class Solver:
         self._check(self._lib.gmgs_phase_times(self._h, d))
         return {"create": d[0], "bc_setup": d[1], "solve": d[2], "stress": d[3]}
 
+    def set_profiling(self, enable: bool = True):
+        self._check(self._lib.gmgs_set_profiling(self._h, int(bool(enable))))
+
+    def kernel_time(self, kernel: int = 0):
+        """(launches, total ms, algorithmic bytes) recorded since set_profiling(True)."""
+        n = C.c_int64()
+        ms = C.c_double()
+        by = C.c_double()
+        self._check(self._lib.gmgs_kernel_time(self._h, kernel, C.byref(n), C.byref(ms), C.byref(by)))
+        return n.value, ms.value, by.value
+
     def set_stream(self, stream_ptr: int | None):
         self._check(self._lib.gmgs_set_stream(self._h, C.c_void_p(stream_ptr or 0)))
 

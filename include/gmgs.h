@@ -142,6 +142,13 @@ int gmgs_set_tolerance(gmgs_handle* h, double tol, int32_t max_it);
 int gmgs_device_bytes(const gmgs_handle* h, int64_t* out);   /* device memory held by the handle */
 int gmgs_launch_count(const gmgs_handle* h, int64_t* out);   /* kernels launched so far */
 int gmgs_phase_times(const gmgs_handle* h, double out[4]);   /* ms: create, bc-setup, last solve, last stress */
+/* Kernel timing with CUDA events on the handle's stream (diagnostics).
+ * gmgs_set_profiling(h, 1) clears the records and starts recording;
+ * gmgs_kernel_time() sums them.  kernel: 0 = finest-level K*x launches,
+ * 1 = whole V-cycles, 2 = whole CG iterations.  bytes: algorithmic bytes of
+ * the recorded launches (kernel 0 only). */
+int gmgs_set_profiling(gmgs_handle* h, int32_t enable);
+int gmgs_kernel_time(gmgs_handle* h, int32_t kernel, int64_t* launches, double* total_ms, double* bytes);
 const char* gmgs_last_error(const gmgs_handle* h);
 const char* gmgs_status_string(int status);
 void gmgs_destroy(gmgs_handle* h);

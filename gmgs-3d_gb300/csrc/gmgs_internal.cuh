@@ -138,6 +138,7 @@ struct Level {
     DevBuf node_count;        // finest level: solid elements per node (numNod2ElesVec_)
     // V-cycle work vectors (3 planes each), precision of the V-cycle
     DevBuf vr, vrp, vdx, vx, vy;
+    DevBuf wdinv32;           // mixed path: omega / diag in FP32
 };
 
 // Per-launch CUDA-event timing of selected kernels (diagnostics; off by default).

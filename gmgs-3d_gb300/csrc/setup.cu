@@ -332,6 +332,23 @@ __global__ void k_node_flags(Grid g, const uint8_t* __restrict__ emask, uint8_t*
     }
 }
 
+// nodes whose 8 elements all carry the level's uniform matrix kscale * Ke0
+__global__ void k_interior_flags(Grid g, const uint8_t* __restrict__ emask, const int32_t* __restrict__ etype,
+                                 uint8_t* __restrict__ nflag) {
+    GRID_STRIDE(s, g.slots) {
+        uint8_t f = nflag[s] & (uint8_t)~NF_INTERIOR;
+        if (f & NF_SOLID) {
+            bool all = true;
+            for (int e = 0; e < 8; ++e) {
+                const int64_t es = s - (e & 1) - ((e >> 1) & 1) * g.sx() - (e >> 2) * g.sz();
+                all = all && emask[es] && (!etype || etype[es] == 0);
+            }
+            if (all) f |= NF_INTERIOR;
+        }
+        nflag[s] = f;
+    }
+}
+
 __global__ void k_flag_to_count(int64_t n, const uint8_t* __restrict__ f, uint8_t bit, int32_t* __restrict__ out) {
     GRID_STRIDE(i, n) out[i] = (f[i] & bit) ? 1 : 0;
 }
@@ -442,7 +459,7 @@ __global__ void k_diag(Grid g, const uint8_t* __restrict__ emask, const uint8_t*
 // boundary conditions
 // ---------------------------------------------------------------------------
 __global__ void k_clear_fixed(int64_t n, uint8_t* f) {
-    GRID_STRIDE(i, n) f[i] &= NF_SOLID;
+    GRID_STRIDE(i, n) f[i] &= (NF_SOLID | NF_INTERIOR);
 }
 __global__ void k_set_fixed(int64_t n, const int32_t* __restrict__ ids, const int32_t* __restrict__ node_slot,
                             uint8_t* __restrict__ f) {
@@ -460,8 +477,8 @@ __global__ void k_set_loads(int64_t n, const int32_t* __restrict__ ids, const do
 // coarse fixed DOFs: restricted indicator != 0 (SetupSolver.m:247-254)
 __global__ void k_fixed_from_indicator(int64_t S, const double* __restrict__ ind, uint8_t* __restrict__ f) {
     GRID_STRIDE(s, S) {
-        uint8_t v = f[s] & NF_SOLID;
-        if (v) {
+        uint8_t v = f[s] & (NF_SOLID | NF_INTERIOR);
+        if (v & NF_SOLID) {
             if (ind[s] != 0.0) v |= NF_FIX_X;
             if (ind[s + S] != 0.0) v |= NF_FIX_Y;
             if (ind[s + 2 * S] != 0.0) v |= NF_FIX_Z;
@@ -674,6 +691,17 @@ void build_operators(Model& M) {
         for (int j = 0; j < 24; ++j) KeT[i * 24 + j] = Ke[j * 24 + i];   // row = output DOF
     std::copy(KeT, KeT + KE, M.ke0_rows);
     upload_ke0(KeT);
+    make_stencil(KeT, M.coef);
+    for (int l = 0; l < L; ++l) {
+        Level& lv = M.levels[l];
+        const bool uniform_ok = !(l == 0 && lv.escale64.p);
+        if (uniform_ok) {
+            k_interior_flags<<<blocks_for(c, lv.g.slots), 256, 0, c.stream>>>(lv.g, lv.emask.as<uint8_t>(),
+                                                                               lv.etype.as<int32_t>(),
+                                                                               lv.nflag.as<uint8_t>());
+            GMGS_LAUNCHED(c);
+        }
+    }
     M.ke0_dev = dalloc(KE * sizeof(double));
     GMGS_CUDA(cudaMemcpyAsync(M.ke0_dev.p, KeT, KE * sizeof(double), cudaMemcpyHostToDevice, c.stream));
     const double* ke0 = M.ke0_dev.as<double>();

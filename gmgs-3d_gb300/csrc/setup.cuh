@@ -2,6 +2,7 @@
 // the C ABI (api.cu).
 #pragma once
 
+#include "fine.cuh"
 #include "gmgs_internal.cuh"
 
 namespace gmgs {
@@ -29,6 +30,8 @@ struct Model {
     // outer CG work vectors
     DevBuf cg_x, cg_r, cg_p, cg_dx, cg_q64, cg_y64, cg_z64;   // FP64 path
     DevBuf cg_q32, cg_y32, cg_z32, cg_r32;                     // mixed path
+    DevBuf cg_r64b, cg_pa, cg_pb;                              // mixed path double buffers
+    Coef32 coef{};                                             // FP32 stencil + element matrix
     DevBuf scal;           // device scalars (see solver.cu)
     DevBuf dot_partials, dot_ticket;
     double* scal_host = nullptr;   // pinned

@@ -5,6 +5,7 @@
 // mixed path keeps x, r, p, the dot products and the coarsest solve in FP64
 // and runs the V-cycle (smoothers, transfers, level matvecs) in FP32; the
 // CG's own matvecs read FP64 vectors and compute in FP32.
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 
@@ -19,44 +20,6 @@ static void zalloc(Ctx& c, DevBuf& b, size_t bytes) {
     GMGS_CUDA(cudaMemsetAsync(b.p, 0, bytes, c.stream));
 }
 
-void alloc_work(Model& M) {
-    Ctx& c = M.ctx;
-    const bool mixed = M.prm.precision == GMGS_MIXED;
-    const size_t T = mixed ? sizeof(float) : sizeof(double);
-    for (int l = 0; l < M.num_levels; ++l) {
-        Level& lv = M.levels[l];
-        const size_t n3 = 3 * (size_t)lv.g.slots;
-        if (l > 0) zalloc(c, lv.vr, n3 * T);
-        zalloc(c, lv.vx, n3 * T);
-        if (l < M.num_levels - 1) {
-            zalloc(c, lv.vrp, n3 * T);
-            zalloc(c, lv.vdx, n3 * T);
-            zalloc(c, lv.vy, n3 * T);
-        }
-    }
-    const size_t n3 = 3 * (size_t)M.levels[0].g.slots;
-    zalloc(c, M.cg_x, n3 * 8);
-    zalloc(c, M.cg_r, n3 * 8);
-    zalloc(c, M.cg_p, n3 * 8);
-    zalloc(c, M.cg_dx, n3 * 8);
-    if (mixed) {
-        zalloc(c, M.cg_q32, n3 * 4);
-        zalloc(c, M.cg_y32, n3 * 4);
-        zalloc(c, M.cg_z32, n3 * 4);
-        zalloc(c, M.cg_r32, n3 * 4);
-    } else {
-        zalloc(c, M.cg_q64, n3 * 8);
-        zalloc(c, M.cg_y64, n3 * 8);
-        zalloc(c, M.cg_z64, n3 * 8);
-    }
-    zalloc(c, M.scal, SC_N * sizeof(double));
-    M.dot_blocks = M.ctx.num_sms * 4;
-    zalloc(c, M.dot_partials, M.dot_blocks * sizeof(double));
-    zalloc(c, M.dot_ticket, sizeof(unsigned int));
-    if (!M.scal_host) GMGS_CUDA(cudaMallocHost(&M.scal_host, SC_N * sizeof(double)));
-    GMGS_CUDA(cudaStreamSynchronize(c.stream));
-}
-
 // level-0 matvec with optional event timing; algorithmic bytes: read x and
 // write y at every solid node, one mask byte per solid element and node
 template <typename Tc, typename Tin, typename Tout>
@@ -66,6 +29,53 @@ static void fine_matvec(Model& M, const Tin* x, Tout* y) {
     M.ctx.mark(PK_FINE_MATVEC, false);
     launch_matvec<Tc, Tin, Tout>(M.ctx, view<Tc>(l0, M.prm.omega), x, y, l0.kscale);
     M.ctx.mark(PK_FINE_MATVEC, true, bytes);
+}
+
+void alloc_work(Model& M) {
+    Ctx& c = M.ctx;
+    const bool mixed = M.prm.precision == GMGS_MIXED;
+    const size_t T = mixed ? sizeof(float) : sizeof(double);
+    const int L = M.num_levels;
+    for (int l = 0; l < L; ++l) {
+        Level& lv = M.levels[l];
+        const size_t n3 = 3 * (size_t)lv.g.slots;
+        if (l > 0) zalloc(c, lv.vr, n3 * T);
+        if (l > 0 || !mixed) zalloc(c, lv.vx, n3 * T);
+        if (l < L - 1) {
+            zalloc(c, lv.vrp, n3 * T);
+            if (!mixed) {
+                zalloc(c, lv.vdx, n3 * T);
+                zalloc(c, lv.vy, n3 * T);
+            } else {
+                if (lv.wdinv32.bytes < n3 * 4) lv.wdinv32 = dalloc(n3 * 4);
+                launch_wdinv(c, (int64_t)n3, lv.diag64.as<double>(), M.prm.omega, lv.wdinv32.as<float>());
+            }
+        }
+    }
+    const size_t n3 = 3 * (size_t)M.levels[0].g.slots;
+    zalloc(c, M.cg_x, n3 * 8);
+    zalloc(c, M.cg_r, n3 * 8);
+    if (mixed) {
+        zalloc(c, M.cg_r64b, n3 * 8);
+        zalloc(c, M.cg_pa, n3 * 4);
+        zalloc(c, M.cg_pb, n3 * 4);
+        zalloc(c, M.cg_q32, n3 * 4);
+        zalloc(c, M.cg_z32, n3 * 4);
+        zalloc(c, M.cg_r32, n3 * 4);
+    } else {
+        zalloc(c, M.cg_p, n3 * 8);
+        zalloc(c, M.cg_dx, n3 * 8);
+        zalloc(c, M.cg_q64, n3 * 8);
+        zalloc(c, M.cg_y64, n3 * 8);
+        zalloc(c, M.cg_z64, n3 * 8);
+    }
+    zalloc(c, M.scal, SC_N * sizeof(double));
+    M.dot_blocks = M.ctx.num_sms * 4;
+    const int maxb = std::max({M.dot_blocks, fine_grid_blocks(M.levels[0].g), up32_grid_blocks(M.levels[0].g)});
+    zalloc(c, M.dot_partials, (size_t)maxb * sizeof(double));
+    zalloc(c, M.dot_ticket, sizeof(unsigned int));
+    if (!M.scal_host) GMGS_CUDA(cudaMallocHost(&M.scal_host, SC_N * sizeof(double)));
+    GMGS_CUDA(cudaStreamSynchronize(c.stream));
 }
 
 static DotScratch dots(Model& M) {
@@ -107,11 +117,13 @@ static void vcycle(Model& M, const T* r0, T* z) {
     c.mark(PK_VCYCLE, true);
 }
 
+static void vcycle32(Model& M, const float* r32, float* z, const double* r64, int dot_slot);
+
 void vcycle_apply(Model& M, const double* r, double* z) {
     const int64_t n3 = 3 * M.levels[0].g.slots;
     if (M.prm.precision == GMGS_MIXED) {
         launch_copy<float, double>(M.ctx, n3, M.cg_r32.as<float>(), r);
-        vcycle<float>(M, M.cg_r32.as<float>(), M.cg_z32.as<float>());
+        vcycle32(M, M.cg_r32.as<float>(), M.cg_z32.as<float>(), nullptr, 0);
         launch_copy<double, float>(M.ctx, n3, z, M.cg_z32.as<float>());
     } else {
         vcycle<double>(M, r, z);
@@ -125,8 +137,168 @@ void apply_operator_dense(Model& M, int level, const double* x, double* y) {
     launch_matvec<double, double, double>(M.ctx, view<double>(lv, M.prm.omega), x, y, lv.kscale);
 }
 
+
+// ---------------------------------------------------------------------------
+// mixed path: FP32 V-cycle on the fused tiled kernels
+// ---------------------------------------------------------------------------
+static FineLevel fine_level(const Level& lv) {
+    FineLevel f;
+    f.g = lv.g;
+    f.emask = lv.emask.as<uint8_t>();
+    f.nflag = lv.nflag.as<uint8_t>();
+    f.etype = lv.etype.as<int32_t>();
+    f.Ks = lv.Ks32.as<float>();
+    f.escale = lv.escale32.as<float>();
+    f.kscale = (float)lv.kscale;
+    return f;
+}
+
+static DotOut dot_out(Model& M, int slot) {
+    DotOut d;
+    d.partials = M.dot_partials.as<double>();
+    d.ticket = M.dot_ticket.as<unsigned int>();
+    d.out = M.scal.as<double>() + slot;
+    return d;
+}
+
+// z = V(r32); the level-1 up-sweep also accumulates r64 . z into scal[dot_slot]
+static void vcycle32(Model& M, const float* r32, float* z, const double* r64, int dot_slot) {
+    Ctx& c = M.ctx;
+    const int L = M.num_levels;
+    c.mark(PK_VCYCLE, false);
+    for (int l = 0; l < L - 1; ++l) {
+        Level& lv = M.levels[l];
+        Level& lc = M.levels[l + 1];
+        FineArgs a;
+        a.r32 = l == 0 ? r32 : lv.vr.as<float>();
+        a.wdinv = lv.wdinv32.as<float>();
+        a.out32 = lv.vrp.as<float>();
+        const double bytes = (double)lv.n_node * 3 * 12 + (double)lv.n_elem;
+        if (l == 0) c.mark(PK_FINE_MATVEC, false);
+        launch_fine<FM_VCYCLE_DOWN>(c, fine_level(lv), M.coef, a);
+        if (l == 0) c.mark(PK_FINE_MATVEC, true, bytes);
+        launch_restrict<float>(c, lv.g, lc.g, lc.nflag.as<uint8_t>(), lv.vrp.as<float>(), lc.vr.as<float>());
+    }
+    Level& lc = M.levels[L - 1];
+    launch_gather<float>(c, M.nfree, M.free_idx.as<int32_t>(), lc.vr.as<float>(), M.cvec_in.as<double>());
+    launch_gemv(c, M.nfree, M.kinv.as<double>(), M.cvec_in.as<double>(), M.cvec_out.as<double>());
+    launch_scatter<float>(c, M.nfree, M.free_idx.as<int32_t>(), M.cvec_out.as<double>(), lc.vx.as<float>());
+    for (int l = L - 2; l >= 0; --l) {
+        Level& lv = M.levels[l];
+        const DotOut d = dot_out(M, dot_slot);
+        launch_up32(c, lv.g, M.levels[l + 1].g, lv.nflag.as<uint8_t>(), lv.wdinv32.as<float>(),
+                    l == 0 ? r32 : lv.vr.as<float>(), lv.vrp.as<float>(), M.levels[l + 1].vx.as<float>(),
+                    l == 0 ? z : lv.vx.as<float>(), l == 0, l == 0 ? r64 : nullptr, (l == 0 && r64) ? &d : nullptr);
+    }
+    c.mark(PK_VCYCLE, true);
+}
+
+static int pcg_mixed(Model& M, const double* b, double* x, int32_t* iters_out, double* relres_out, double* hist) {
+    Ctx& c = M.ctx;
+    Level& l0 = M.levels[0];
+    const int64_t n3 = 3 * l0.g.slots;
+    double* scal = M.scal.as<double>();
+    const DotScratch ds = dots(M);
+    double* ra = M.cg_r.as<double>();
+    double* rb = M.cg_r64b.as<double>();
+    float* pa = M.cg_pa.as<float>();
+    float* pb = M.cg_pb.as<float>();
+    const FineLevel f0 = fine_level(l0);
+
+    launch_dot<double, double>(c, ds, n3, b, b, scal + SC_BB);
+    GMGS_CUDA(cudaMemcpyAsync(M.scal_host + SC_BB, scal + SC_BB, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    GMGS_CUDA(cudaMemsetAsync(x, 0, n3 * sizeof(double), c.stream));
+    GMGS_CUDA(cudaMemcpyAsync(ra, b, n3 * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
+    GMGS_CUDA(cudaStreamSynchronize(c.stream));
+    const double normB = std::sqrt(M.scal_host[SC_BB]);
+    if (normB == 0.0) {
+        if (iters_out) *iters_out = 0;
+        if (relres_out) *relres_out = 0;
+        M.last_iters = 0;
+        M.last_relres = 0;
+        return GMGS_OK;
+    }
+    if (!std::isfinite(normB)) throw Error(GMGS_ERR_NONFINITE, "non-finite load vector");
+    const double jbytes = (double)l0.n_node * 3 * (8 + 8 + 4 + 8 + 8 + 4) + (double)l0.n_elem;
+    const double pbytes = (double)l0.n_node * 3 * (4 + 4 + 4 + 4) + (double)l0.n_elem;
+
+    const auto t0 = std::chrono::steady_clock::now();
+    int its = 0, nhist = 0;
+    double resnorm = INFINITY;
+    int status = GMGS_ERR_MAX_ITERATIONS;
+    while (its <= M.prm.max_it) {
+        c.mark(PK_CG_ITER, false);
+        {   // [x, r1] = JacobiSmoother(var)   (CG_solver.m:18-19)
+            FineArgs a;
+            a.r64 = ra;
+            a.wdinv = l0.wdinv32.as<float>();
+            a.x64 = x;
+            a.r64out = rb;
+            a.r32out = M.cg_r32.as<float>();
+            c.mark(PK_FINE_MATVEC, false);
+            launch_fine<FM_CG_JACOBI>(c, f0, M.coef, a);
+            c.mark(PK_FINE_MATVEC, true, jbytes);
+            std::swap(ra, rb);
+        }
+        ++its;
+        const int cur = its & 1;
+        vcycle32(M, M.cg_r32.as<float>(), M.cg_z32.as<float>(), ra, cur);     // z2 = PtV(r1), r1'z2
+        {   // p2 = z2 + beta p1; q = A p2; p2'q   (CG_solver.m:23-31)
+            FineArgs a;
+            a.z32 = M.cg_z32.as<float>();
+            a.pold = pa;
+            a.pout = pb;
+            a.scal = scal;
+            a.cur = cur;
+            a.first = its == 1;
+            a.out32 = M.cg_q32.as<float>();
+            a.dot = dot_out(M, SC_PQ);
+            c.mark(PK_FINE_MATVEC, false);
+            launch_fine<FM_CG_DIRECTION>(c, f0, M.coef, a);
+            c.mark(PK_FINE_MATVEC, true, pbytes);
+            std::swap(pa, pb);
+        }
+        // x += alpha p2; r2 = r1 - alpha q; r2'r2   (CG_solver.m:31-35)
+        launch_xr32(c, n3, x, ra, pa, M.cg_q32.as<float>(), scal, cur, dot_out(M, SC_RR), M.dot_blocks);
+        c.mark(PK_CG_ITER, true);
+        GMGS_CUDA(cudaMemcpyAsync(M.scal_host + SC_RR, scal + SC_RR, sizeof(double), cudaMemcpyDeviceToHost,
+                                  c.stream));
+        GMGS_CUDA(cudaStreamSynchronize(c.stream));
+        resnorm = std::sqrt(M.scal_host[SC_RR]) / normB;
+        if (M.prm.verbose) std::printf(" It.: %4d Res.: %16.6e\n", its, resnorm);
+        if (!std::isfinite(resnorm)) {
+            status = GMGS_ERR_NONFINITE;
+            break;
+        }
+        if (resnorm < M.prm.tol) {
+            status = GMGS_OK;
+            if (M.prm.verbose)
+                std::printf("CG solver converged at iteration%5d to a solution with relative residual%16.6e\n", its,
+                            resnorm);
+            break;
+        }
+        if (hist) {
+            const double t = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            hist[3 * nhist + 0] = its;
+            hist[3 * nhist + 1] = t;
+            hist[3 * nhist + 2] = resnorm;
+        }
+        ++nhist;
+    }
+    // keep the residual in the primary buffer for callers that read it
+    if (ra != M.cg_r.as<double>())
+        GMGS_CUDA(cudaMemcpyAsync(M.cg_r.p, ra, n3 * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
+    if (status == GMGS_ERR_MAX_ITERATIONS && M.prm.verbose) std::printf("Exceed the maximum iterate numbers\n");
+    if (iters_out) *iters_out = its;
+    if (relres_out) *relres_out = resnorm;
+    M.last_iters = its;
+    M.last_relres = resnorm;
+    return status;
+}
+
 // CG_solver.m:1-56 with the Jacobi step before each preconditioner call.
 int pcg_solve(Model& M, const double* b, double* x, int32_t* iters_out, double* relres_out, double* hist) {
+    if (M.prm.precision == GMGS_MIXED) return pcg_mixed(M, b, x, iters_out, relres_out, hist);
     Ctx& c = M.ctx;
     Level& l0 = M.levels[0];
     const int64_t n3 = 3 * l0.g.slots;

@@ -85,7 +85,7 @@ int64_t model_bytes(const gmgs::Model& M) {
             b += (int64_t)d->bytes;
     for (const gmgs::DevBuf* d : {&M.ke0_dev, &M.rho, &M.F, &M.U, &M.free_idx, &M.kinv, &M.cvec_in, &M.cvec_out,
                                   &M.cg_x, &M.cg_r, &M.cg_p, &M.cg_dx, &M.cg_q64, &M.cg_y64, &M.cg_z64, &M.cg_q32,
-                                  &M.cg_y32, &M.cg_z32, &M.cg_r32, &M.scal, &M.dot_partials, &M.dot_ticket})
+                                  &M.cg_y32, &M.cg_z32, &M.cg_r32, &M.cg_r64b, &M.cg_pa, &M.cg_pb, &M.cg_dxp, &M.scal, &M.dot_partials, &M.dot_ticket})
         b += (int64_t)d->bytes;
     return b;
 }

@@ -1,10 +1,10 @@
 // Tiled FP32 operator kernels of the mixed-precision path.
 //
-// One CTA owns a 32 x 8 x 4 block of nodes (y fastest) and stages the input
-// field on the block plus a one-node halo (34 x 10 x 6 points, 3 components,
-// 24 KB) in shared memory; the field is computed while staging from the
-// kernel's inputs (the Jacobi step omega*D^-1 r, or the CG direction
-// z + beta p), so no intermediate vector goes through HBM.
+// One CTA owns a 32 x 8 column of nodes (y fastest) and streams it through z
+// with a three-plane ring of the input field plus a one-node halo in shared
+// memory; the field is computed while staging from the kernel's inputs (the
+// Jacobi step omega*D^-1 r, or the CG direction z + beta p), so no
+// intermediate vector goes through HBM.
 //
 // Interior nodes (all 8 surrounding elements carry the level's uniform
 // matrix) use the assembled 27-point stencil in second-difference form
@@ -22,11 +22,9 @@
 
 namespace gmgs {
 
-constexpr int TY = 32, TX = 8, TZ = 4;
-constexpr int HY = TY + 2, HX = TX + 2, HZ = TZ + 2;
-constexpr int TILE = HY * HX * HZ;
+constexpr int TY = 32, TX = 8;
+constexpr int HY = TY + 2, HX = TX + 2;
 constexpr int NT = TY * TX;
-constexpr int SX = HY, SZ = HY * HX;
 
 // displacement component a (0 = x, 1 = y, 2 = z) of stencil offset k = (dz+1)*9 + (dx+1)*3 + (dy+1)
 __host__ __device__ constexpr int off_y(int k) { return k % 3 - 1; }
@@ -64,78 +62,6 @@ void make_stencil(const double* ke_rows, Coef32& cf) {
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ bool in_halo_grid(const Grid& g, int iy, int ix, int iz) {
     return iy >= -1 && ix >= -1 && iz >= -1 && iy <= g.ny + 1 && ix <= g.nx + 1 && iz <= g.nz + 1;
-}
-
-// interior node: second-difference form of the uniform stencil
-__device__ __forceinline__ void interior(const Coef32& cf, const float* __restrict__ sv, int p, float& y0, float& y1,
-                                         float& y2) {
-    const float c[3] = {sv[p], sv[p + TILE], sv[p + 2 * TILE]};
-    float acc[3] = {0.f, 0.f, 0.f};
-#pragma unroll
-    for (int k = 14; k < 27; ++k) {
-        const int o = off_y(k) + off_x(k) * SX + off_z(k) * SZ;
-        float d[3];
-#pragma unroll
-        for (int b = 0; b < 3; ++b) d[b] = (sv[p + o + b * TILE] - c[b]) + (sv[p - o + b * TILE] - c[b]);
-#pragma unroll
-        for (int a = 0; a < 3; ++a)
-#pragma unroll
-            for (int b = 0; b < 3; ++b)
-                if (s_nonzero(k, a, b)) acc[a] = fmaf(cf.S[k * 9 + 3 * a + b], d[b], acc[a]);
-    }
-    y0 = acc[0]; y1 = acc[1]; y2 = acc[2];
-}
-
-// one element's rows for the node at local corner CI, first-difference form
-template <int CI, bool GLOBALK>
-__device__ __forceinline__ void elem_rows(const float* __restrict__ K, float s, const float* __restrict__ sv, int pe,
-                                          const float c[3], float acc[3]) {
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-        if (j == CI) continue;
-        const int q = pe + corner_y(j) + corner_x(j) * SX + corner_z(j) * SZ;
-        const float d0 = sv[q] - c[0], d1 = sv[q + TILE] - c[1], d2 = sv[q + 2 * TILE] - c[2];
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            const int r = (3 * CI + a) * 24 + 3 * j;
-            float t = K[r] * d0;
-            t = fmaf(K[r + 1], d1, t);
-            t = fmaf(K[r + 2], d2, t);
-            acc[a] = fmaf(s, t, acc[a]);
-        }
-    }
-}
-
-template <int E>
-__device__ __forceinline__ void boundary_elem(const FineLevel& L, const Coef32& cf, const float* __restrict__ sv, int p,
-                                              int64_t n, const float c[3], float acc[3]) {
-    constexpr int A = E & 1, B = (E >> 1) & 1, C = E >> 2;
-    constexpr int CI = corner_of(A, B, C);
-    const int64_t es = n - A - B * L.g.sx() - C * L.g.sz();
-    if (!L.emask[es]) return;
-    const int pe = p - A - B * SX - C * SZ;      // element origin in the tile
-    const int t = L.etype ? L.etype[es] : 0;
-    if (t > 0) {
-        elem_rows<CI, true>(L.Ks + (int64_t)(t - 1) * KE, 1.0f, sv, pe, c, acc);
-    } else {
-        const float s = L.escale ? L.kscale * L.escale[es] : L.kscale;
-        elem_rows<CI, false>(cf.K, s, sv, pe, c, acc);
-    }
-}
-
-__device__ __forceinline__ void boundary(const FineLevel& L, const Coef32& cf, const float* __restrict__ sv, int p,
-                                         int64_t n, float& y0, float& y1, float& y2) {
-    const float c[3] = {sv[p], sv[p + TILE], sv[p + 2 * TILE]};
-    float acc[3] = {0.f, 0.f, 0.f};
-    boundary_elem<0>(L, cf, sv, p, n, c, acc);
-    boundary_elem<1>(L, cf, sv, p, n, c, acc);
-    boundary_elem<2>(L, cf, sv, p, n, c, acc);
-    boundary_elem<3>(L, cf, sv, p, n, c, acc);
-    boundary_elem<4>(L, cf, sv, p, n, c, acc);
-    boundary_elem<5>(L, cf, sv, p, n, c, acc);
-    boundary_elem<6>(L, cf, sv, p, n, c, acc);
-    boundary_elem<7>(L, cf, sv, p, n, c, acc);
-    y0 = acc[0]; y1 = acc[1]; y2 = acc[2];
 }
 
 __device__ __forceinline__ double block_sum_d(double v, double* sh) {
@@ -181,106 +107,243 @@ __device__ void grid_dot_finish(double v, const DotOut& d, double* sh) {
 }
 
 // ---------------------------------------------------------------------------
-// the fused kernel
+// the fused streaming kernel
+//
+// A CTA of 32 x 8 threads owns a 32 x 8 column of nodes and walks it through
+// ZC planes in z.  Shared memory holds a ring of three (32+2) x (8+2) planes
+// of the input field; the plane two steps ahead is loaded (and transformed)
+// into registers while the current plane is computed, so global loads
+// overlap the stencil arithmetic.
 // ---------------------------------------------------------------------------
+constexpr int PLANE = HY * HX;                 // 340 points
+constexpr int PPT = (PLANE + NT - 1) / NT;     // points per thread and plane
+
+struct PlaneRegs {
+    float v[PPT][3];
+};
+
+struct Scalars {
+    float beta;      // FM_CG_DIRECTION
+    double alpha;    // FM_CG_UPDATE_JACOBI
+};
+
 template <int MODE>
-__global__ void __launch_bounds__(NT, 2) k_fine(FineLevel L, const __grid_constant__ Coef32 cf, FineArgs a) {
-    __shared__ float sv[3 * TILE];
+__device__ __forceinline__ void fetch_plane(const Grid& g, const FineArgs& a, const Scalars& sc, int y0, int x0, int iz,
+                                            int tid, PlaneRegs& pr) {
+    const int64_t S = g.slots;
+#pragma unroll
+    for (int k = 0; k < PPT; ++k) {
+        const int t = tid + k * NT;
+        const int ly = t % HY, lx = t / HY;
+        const int iy = y0 - 1 + ly, ix = x0 - 1 + lx;
+        float v[3] = {0.f, 0.f, 0.f};
+        if (t < PLANE && in_halo_grid(g, iy, ix, iz)) {
+            const int64_t s = g.slot(iy, ix, iz);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const int64_t i = s + c * S;
+                if (MODE == FM_PLAIN) {
+                    v[c] = a.v[i];
+                } else if (MODE == FM_VCYCLE_DOWN) {
+                    v[c] = a.r32[i] * a.wdinv[i];
+                } else if (MODE == FM_CG_UPDATE_JACOBI) {
+                    const double rm = a.first ? a.r64[i] : a.r64[i] - sc.alpha * (double)a.q32[i];
+                    v[c] = (float)rm * a.wdinv[i];
+                } else {   // FM_CG_DIRECTION
+                    v[c] = a.first ? a.z32[i] : fmaf(sc.beta, a.pold[i], a.z32[i]);
+                }
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) pr.v[k][c] = v[c];
+    }
+}
+
+__device__ __forceinline__ void store_plane(float* __restrict__ ring, int tid, const PlaneRegs& pr) {
+#pragma unroll
+    for (int k = 0; k < PPT; ++k) {
+        const int t = tid + k * NT;
+        if (t < PLANE) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) ring[c * PLANE + t] = pr.v[k][c];
+        }
+    }
+}
+
+// interior node, second-difference form; P[0..2] = planes z-1, z, z+1, p = in-plane index
+__device__ __forceinline__ void interior_s(const Coef32& cf, const float* const P[3], int p, float acc[3]) {
+    const float c[3] = {P[1][p], P[1][p + PLANE], P[1][p + 2 * PLANE]};
+    acc[0] = acc[1] = acc[2] = 0.f;
+#pragma unroll
+    for (int k = 14; k < 27; ++k) {
+        const int o = off_y(k) + off_x(k) * HY;
+        const float* up = P[1 + off_z(k)];
+        const float* dn = P[1 - off_z(k)];
+        float d[3];
+#pragma unroll
+        for (int b = 0; b < 3; ++b) d[b] = (up[p + o + b * PLANE] - c[b]) + (dn[p - o + b * PLANE] - c[b]);
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b)
+                if (s_nonzero(k, a, b)) acc[a] = fmaf(cf.S[k * 9 + 3 * a + b], d[b], acc[a]);
+    }
+}
+
+template <int CI>
+__device__ __forceinline__ void elem_rows_s(const float* __restrict__ K, float s, const float* const P[3], int p, int A,
+                                            int B, int C, const float c[3], float acc[3]) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        if (j == CI) continue;
+        const int dy = corner_y(j) - A, dx = corner_x(j) - B, dz = corner_z(j) - C;
+        const float* pl = P[1 + dz];
+        const int q = p + dy + dx * HY;
+        const float d0 = pl[q] - c[0], d1 = pl[q + PLANE] - c[1], d2 = pl[q + 2 * PLANE] - c[2];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const int r = (3 * CI + a) * 24 + 3 * j;
+            float t = K[r] * d0;
+            t = fmaf(K[r + 1], d1, t);
+            t = fmaf(K[r + 2], d2, t);
+            acc[a] = fmaf(s, t, acc[a]);
+        }
+    }
+}
+
+template <int E>
+__device__ __forceinline__ void boundary_elem_s(const FineLevel& L, const Coef32& cf, const float* const P[3], int p,
+                                                int64_t n, const float c[3], float acc[3]) {
+    constexpr int A = E & 1, B = (E >> 1) & 1, C = E >> 2;
+    constexpr int CI = corner_of(A, B, C);
+    const int64_t es = n - A - B * L.g.sx() - C * L.g.sz();
+    if (!L.emask[es]) return;
+    const int t = L.etype ? L.etype[es] : 0;
+    if (t > 0) {
+        elem_rows_s<CI>(L.Ks + (int64_t)(t - 1) * KE, 1.0f, P, p, A, B, C, c, acc);
+    } else {
+        const float s = L.escale ? L.kscale * L.escale[es] : L.kscale;
+        elem_rows_s<CI>(cf.K, s, P, p, A, B, C, c, acc);
+    }
+}
+
+__device__ __noinline__ void boundary_s(const FineLevel& L, const Coef32& cf, const float* const P[3], int p, int64_t n,
+                                        float acc[3]) {
+    const float c[3] = {P[1][p], P[1][p + PLANE], P[1][p + 2 * PLANE]};
+    acc[0] = acc[1] = acc[2] = 0.f;
+    boundary_elem_s<0>(L, cf, P, p, n, c, acc);
+    boundary_elem_s<1>(L, cf, P, p, n, c, acc);
+    boundary_elem_s<2>(L, cf, P, p, n, c, acc);
+    boundary_elem_s<3>(L, cf, P, p, n, c, acc);
+    boundary_elem_s<4>(L, cf, P, p, n, c, acc);
+    boundary_elem_s<5>(L, cf, P, p, n, c, acc);
+    boundary_elem_s<6>(L, cf, P, p, n, c, acc);
+    boundary_elem_s<7>(L, cf, P, p, n, c, acc);
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(NT, 3) k_fine(FineLevel L, const __grid_constant__ Coef32 cf, FineArgs a, int zc) {
+    __shared__ float ring[3][3 * PLANE];
     __shared__ double sh[32];
     const Grid& g = L.g;
     const int64_t S = g.slots;
-    const int y0 = blockIdx.x * TY, x0 = blockIdx.y * TX, z0 = blockIdx.z * TZ;
+    const int y0 = blockIdx.x * TY, x0 = blockIdx.y * TX;
+    const int zb = blockIdx.z * zc;
+    const int ze = min(zb + zc, g.nz + 1);        // node planes [zb, ze)
     const int tid = threadIdx.x + threadIdx.y * TY;
 
-    float beta = 0.f;
-    if (MODE == FM_CG_DIRECTION && !a.first) beta = (float)(a.scal[a.cur] / a.scal[a.cur ^ 1]);
+    Scalars sc;
+    sc.beta = 0.f;
+    sc.alpha = 0.0;
+    if (MODE == FM_CG_DIRECTION && !a.first) sc.beta = (float)(a.scal[a.cur] / a.scal[a.cur ^ 1]);
+    if (MODE == FM_CG_UPDATE_JACOBI && !a.first) sc.alpha = a.scal[a.cur] / a.scal[2];
 
-    // stage the input field v on the tile + halo
-    for (int t = tid; t < TILE; t += NT) {
-        const int ly = t % HY, lx = (t / HY) % HX, lz = t / (HY * HX);
-        const int iy = y0 - 1 + ly, ix = x0 - 1 + lx, iz = z0 - 1 + lz;
-        float v0 = 0.f, v1 = 0.f, v2 = 0.f;
-        if (in_halo_grid(g, iy, ix, iz)) {
-            const int64_t s = g.slot(iy, ix, iz);
-            if (MODE == FM_PLAIN) {
-                v0 = a.v[s]; v1 = a.v[s + S]; v2 = a.v[s + 2 * S];
-            } else if (MODE == FM_VCYCLE_DOWN) {
-                v0 = a.r32[s] * a.wdinv[s];
-                v1 = a.r32[s + S] * a.wdinv[s + S];
-                v2 = a.r32[s + 2 * S] * a.wdinv[s + 2 * S];
-            } else if (MODE == FM_CG_JACOBI) {
-                v0 = (float)a.r64[s] * a.wdinv[s];
-                v1 = (float)a.r64[s + S] * a.wdinv[s + S];
-                v2 = (float)a.r64[s + 2 * S] * a.wdinv[s + 2 * S];
-            } else {   // FM_CG_DIRECTION
-                v0 = a.first ? a.z32[s] : fmaf(beta, a.pold[s], a.z32[s]);
-                v1 = a.first ? a.z32[s + S] : fmaf(beta, a.pold[s + S], a.z32[s + S]);
-                v2 = a.first ? a.z32[s + 2 * S] : fmaf(beta, a.pold[s + 2 * S], a.z32[s + 2 * S]);
-            }
-        }
-        sv[t] = v0;
-        sv[t + TILE] = v1;
-        sv[t + 2 * TILE] = v2;
-    }
-    __syncthreads();
+    PlaneRegs pr;
+    fetch_plane<MODE>(g, a, sc, y0, x0, zb - 1, tid, pr);
+    store_plane(ring[(zb - 1 + 3) % 3], tid, pr);
+    fetch_plane<MODE>(g, a, sc, y0, x0, zb, tid, pr);
+    store_plane(ring[zb % 3], tid, pr);
+    fetch_plane<MODE>(g, a, sc, y0, x0, zb + 1, tid, pr);
 
-    double dot = 0.0;
     const int iy = y0 + threadIdx.x, ix = x0 + threadIdx.y;
+    const bool own = iy <= g.ny && ix <= g.nx;
+    const int p = (threadIdx.x + 1) + (threadIdx.y + 1) * HY;
+    double dot = 0.0;
 #pragma unroll 1
-    for (int kz = 0; kz < TZ; ++kz) {
-        const int iz = z0 + kz;
-        if (iy > g.ny || ix > g.nx || iz > g.nz) break;
-        const int64_t n = g.slot(iy, ix, iz);
-        const uint8_t f = L.nflag[n];
-        if (!(f & NF_SOLID)) continue;
-        const int p = (threadIdx.x + 1) + (threadIdx.y + 1) * SX + (kz + 1) * SZ;
-        float y0v, y1v, y2v;
-        if (f & NF_INTERIOR) {
-            interior(cf, sv, p, y0v, y1v, y2v);
-            y0v *= L.kscale; y1v *= L.kscale; y2v *= L.kscale;
-        } else {
-            boundary(L, cf, sv, p, n, y0v, y1v, y2v);
-        }
-        if (f & NF_FIX_X) y0v = 0.f;
-        if (f & NF_FIX_Y) y1v = 0.f;
-        if (f & NF_FIX_Z) y2v = 0.f;
-        const float yv[3] = {y0v, y1v, y2v};
+    for (int iz = zb; iz < ze; ++iz) {
+        store_plane(ring[(iz + 1) % 3], tid, pr);
+        __syncthreads();
+        if (iz + 2 <= g.nz + 1) fetch_plane<MODE>(g, a, sc, y0, x0, iz + 2, tid, pr);
+        const float* const P[3] = {ring[(iz + 2) % 3], ring[iz % 3], ring[(iz + 1) % 3]};
+        if (own) {
+            const int64_t n = g.slot(iy, ix, iz);
+            const uint8_t f = L.nflag[n];
+            if (f & NF_SOLID) {
+                float y[3];
+                if (f & NF_INTERIOR) {
+                    interior_s(cf, P, p, y);
+                    y[0] *= L.kscale; y[1] *= L.kscale; y[2] *= L.kscale;
+                } else {
+                    boundary_s(L, cf, P, p, n, y);
+                }
+                if (f & NF_FIX_X) y[0] = 0.f;
+                if (f & NF_FIX_Y) y[1] = 0.f;
+                if (f & NF_FIX_Z) y[2] = 0.f;
 #pragma unroll
-        for (int b = 0; b < 3; ++b) {
-            const int64_t i = n + b * S;
-            const float v = sv[p + b * TILE];
-            if (MODE == FM_PLAIN) {
-                a.out32[i] = yv[b];
-            } else if (MODE == FM_VCYCLE_DOWN) {
-                a.out32[i] = a.r32[i] - yv[b];                       // r' = r - A (omega D^-1 r)
-            } else if (MODE == FM_CG_JACOBI) {
-                a.x64[i] += (double)v;                               // x += dx
-                const double rn = a.r64[i] - (double)yv[b];          // r -= A dx
-                a.r64out[i] = rn;
-                a.r32out[i] = (float)rn;
-            } else {
-                a.pout[i] = v;
-                a.out32[i] = yv[b];                                  // q = A p
-                dot += (double)v * (double)yv[b];
+                for (int b = 0; b < 3; ++b) {
+                    const int64_t i = n + b * S;
+                    const float v = P[1][p + b * PLANE];
+                    if (MODE == FM_PLAIN) {
+                        a.out32[i] = y[b];
+                    } else if (MODE == FM_VCYCLE_DOWN) {
+                        a.out32[i] = a.r32[i] - y[b];                    // r' = r - A (omega D^-1 r)
+                    } else if (MODE == FM_CG_UPDATE_JACOBI) {
+                        // previous iteration's update x += alpha p, r -= alpha q (CG_solver.m:32-33),
+                        // then this iteration's Jacobi step (CG_solver.m:18-19), its dx kept pending
+                        const double rm = a.first ? a.r64[i] : a.r64[i] - sc.alpha * (double)a.q32[i];
+                        if (!a.first) a.x64[i] = (a.x64[i] + (double)a.dxp[i]) + sc.alpha * (double)a.pold[i];
+                        a.dxp[i] = v;
+                        const double rn = rm - (double)y[b];
+                        a.r64out[i] = rn;
+                        a.r32out[i] = (float)rn;
+                        dot += rm * rm;
+                    } else {
+                        a.pout[i] = v;
+                        a.out32[i] = y[b];                               // q = A p
+                        dot += (double)v * (double)y[b];
+                    }
+                }
             }
         }
+        __syncthreads();
     }
-    if (MODE == FM_CG_DIRECTION) grid_dot_finish(dot, a.dot, sh);
+    if (MODE == FM_CG_DIRECTION || MODE == FM_CG_UPDATE_JACOBI) grid_dot_finish(dot, a.dot, sh);
+}
+
+static int pick_zc(const Grid& g, const Ctx& c) {
+    const int64_t cols = (int64_t)((g.ny + 1 + TY - 1) / TY) * ((g.nx + 1 + TX - 1) / TX);
+    const int64_t want = (int64_t)c.num_sms * 3 * 6;      // ~6 waves of resident CTAs
+    int64_t zc = (cols * (g.nz + 1) + want - 1) / want;
+    if (zc < 4) zc = 4;
+    if (zc > 64) zc = 64;
+    return (int)zc;
 }
 
 int fine_grid_blocks(const Grid& g) {
-    return ((g.ny + 1 + TY - 1) / TY) * ((g.nx + 1 + TX - 1) / TX) * ((g.nz + 1 + TZ - 1) / TZ);
+    // upper bound over the z-chunk choices (zc >= 4)
+    return ((g.ny + 1 + TY - 1) / TY) * ((g.nx + 1 + TX - 1) / TX) * ((g.nz + 1 + 3) / 4);
 }
 
 template <int MODE>
 void launch_fine(Ctx& c, const FineLevel& L, const Coef32& cf, const FineArgs& a) {
-    dim3 grid((L.g.ny + 1 + TY - 1) / TY, (L.g.nx + 1 + TX - 1) / TX, (L.g.nz + 1 + TZ - 1) / TZ);
-    k_fine<MODE><<<grid, dim3(TY, TX, 1), 0, c.stream>>>(L, cf, a);
+    const int zc = pick_zc(L.g, c);
+    dim3 grid((L.g.ny + 1 + TY - 1) / TY, (L.g.nx + 1 + TX - 1) / TX, (L.g.nz + 1 + zc - 1) / zc);
+    k_fine<MODE><<<grid, dim3(TY, TX, 1), 0, c.stream>>>(L, cf, a, zc);
     GMGS_LAUNCHED(c);
 }
 template void launch_fine<FM_PLAIN>(Ctx&, const FineLevel&, const Coef32&, const FineArgs&);
 template void launch_fine<FM_VCYCLE_DOWN>(Ctx&, const FineLevel&, const Coef32&, const FineArgs&);
-template void launch_fine<FM_CG_JACOBI>(Ctx&, const FineLevel&, const Coef32&, const FineArgs&);
+template void launch_fine<FM_CG_UPDATE_JACOBI>(Ctx&, const FineLevel&, const Coef32&, const FineArgs&);
 template void launch_fine<FM_CG_DIRECTION>(Ctx&, const FineLevel&, const Coef32&, const FineArgs&);
 
 // ---------------------------------------------------------------------------

@@ -30,10 +30,12 @@ struct DotOut {
 };
 
 enum FineMode {
-    FM_PLAIN = 0,          // y = A v
-    FM_VCYCLE_DOWN = 1,    // v = w r, out = r - A v               (Vcycle.m:14, JacobiSmoother.m:5-9)
-    FM_CG_JACOBI = 2,      // v = fl32(w r64), x += v, r -= A v     (CG_solver.m:18-19)
-    FM_CG_DIRECTION = 3    // v = fl32(z + beta p_old), p = v, q = A v, p.q  (CG_solver.m:23-31)
+    FM_PLAIN = 0,             // y = A v
+    FM_VCYCLE_DOWN = 1,       // v = w r, out = r - A v               (Vcycle.m:14, JacobiSmoother.m:5-9)
+    FM_CG_UPDATE_JACOBI = 2,  // previous CG update r_m = r - alpha q, x += dx_prev + alpha p,
+                              // r_m.r_m; then v = fl32(w r_m) kept as the pending dx,
+                              // r = r_m - A v                  (CG_solver.m:31-35, 18-19)
+    FM_CG_DIRECTION = 3       // v = fl32(z + beta p_old), p = v, q = A v, p.q  (CG_solver.m:23-31)
 };
 
 struct FineArgs {
@@ -42,8 +44,10 @@ struct FineArgs {
     const double* r64 = nullptr;     // FM_CG_JACOBI input residual (read on the halo)
     const float* wdinv = nullptr;    // omega / diag (3 planes)
     const float* z32 = nullptr;      // FM_CG_DIRECTION preconditioned residual
-    const float* pold = nullptr;     // FM_CG_DIRECTION previous direction
-    const double* scal = nullptr;    // CG scalars: [0],[1] r.z by parity
+    const float* pold = nullptr;     // previous direction (FM_CG_DIRECTION: p_{k-1}; FM_CG_UPDATE_JACOBI: p_k)
+    const float* q32 = nullptr;      // FM_CG_UPDATE_JACOBI: q = A p of the previous iteration
+    float* dxp = nullptr;            // FM_CG_UPDATE_JACOBI: pending Jacobi step (read, then overwritten)
+    const double* scal = nullptr;    // CG scalars: [0],[1] r.z by parity, [2] p.q
     int cur = 0, first = 0;
     float* out32 = nullptr;          // y / r' / q
     float* pout = nullptr;           // new direction (must not alias pold)

@@ -62,6 +62,7 @@ void alloc_work(Model& M) {
         zalloc(c, M.cg_q32, n3 * 4);
         zalloc(c, M.cg_z32, n3 * 4);
         zalloc(c, M.cg_r32, n3 * 4);
+        zalloc(c, M.cg_dxp, n3 * 4);
     } else {
         zalloc(c, M.cg_p, n3 * 8);
         zalloc(c, M.cg_dx, n3 * 8);
@@ -219,30 +220,46 @@ static int pcg_mixed(Model& M, const double* b, double* x, int32_t* iters_out, d
         return GMGS_OK;
     }
     if (!std::isfinite(normB)) throw Error(GMGS_ERR_NONFINITE, "non-finite load vector");
-    const double jbytes = (double)l0.n_node * 3 * (8 + 8 + 4 + 8 + 8 + 4) + (double)l0.n_elem;
+    const double jbytes = (double)l0.n_node * 3 * (8 + 4 + 4 + 8 + 4 + 4 + 8 + 8 + 4 + 4) + (double)l0.n_elem;
     const double pbytes = (double)l0.n_node * 3 * (4 + 4 + 4 + 4) + (double)l0.n_elem;
+    float* dxp = M.cg_dxp.as<float>();
+    float* q = M.cg_q32.as<float>();
+    float* r32 = M.cg_r32.as<float>();
+
+    // Fused kernel F: the previous iteration's update (x += alpha p, r -= alpha q,
+    // |r|^2 for its convergence test) followed by this iteration's Jacobi step,
+    // whose dx stays pending until the next update, so x is always the
+    // reference's x at the end of the last completed iteration.
+    auto update_jacobi = [&](int first, int cur) {
+        FineArgs a;
+        a.r64 = ra;
+        a.q32 = q;
+        a.pold = pa;
+        a.wdinv = l0.wdinv32.as<float>();
+        a.x64 = x;
+        a.dxp = dxp;
+        a.r64out = rb;
+        a.r32out = r32;
+        a.scal = scal;
+        a.cur = cur;
+        a.first = first;
+        a.dot = dot_out(M, SC_RR);
+        c.mark(PK_FINE_MATVEC, false);
+        launch_fine<FM_CG_UPDATE_JACOBI>(c, f0, M.coef, a);
+        c.mark(PK_FINE_MATVEC, true, jbytes);
+        std::swap(ra, rb);
+    };
 
     const auto t0 = std::chrono::steady_clock::now();
     int its = 0, nhist = 0;
     double resnorm = INFINITY;
     int status = GMGS_ERR_MAX_ITERATIONS;
+    update_jacobi(1, 0);          // [x, r1] = JacobiSmoother(var) of the first iteration (CG_solver.m:18-19)
     while (its <= M.prm.max_it) {
         c.mark(PK_CG_ITER, false);
-        {   // [x, r1] = JacobiSmoother(var)   (CG_solver.m:18-19)
-            FineArgs a;
-            a.r64 = ra;
-            a.wdinv = l0.wdinv32.as<float>();
-            a.x64 = x;
-            a.r64out = rb;
-            a.r32out = M.cg_r32.as<float>();
-            c.mark(PK_FINE_MATVEC, false);
-            launch_fine<FM_CG_JACOBI>(c, f0, M.coef, a);
-            c.mark(PK_FINE_MATVEC, true, jbytes);
-            std::swap(ra, rb);
-        }
         ++its;
         const int cur = its & 1;
-        vcycle32(M, M.cg_r32.as<float>(), M.cg_z32.as<float>(), ra, cur);     // z2 = PtV(r1), r1'z2
+        vcycle32(M, r32, M.cg_z32.as<float>(), ra, cur);     // z2 = PtV(r1), r1'z2   (CG_solver.m:21,26)
         {   // p2 = z2 + beta p1; q = A p2; p2'q   (CG_solver.m:23-31)
             FineArgs a;
             a.z32 = M.cg_z32.as<float>();
@@ -251,15 +268,14 @@ static int pcg_mixed(Model& M, const double* b, double* x, int32_t* iters_out, d
             a.scal = scal;
             a.cur = cur;
             a.first = its == 1;
-            a.out32 = M.cg_q32.as<float>();
+            a.out32 = q;
             a.dot = dot_out(M, SC_PQ);
             c.mark(PK_FINE_MATVEC, false);
             launch_fine<FM_CG_DIRECTION>(c, f0, M.coef, a);
             c.mark(PK_FINE_MATVEC, true, pbytes);
             std::swap(pa, pb);
         }
-        // x += alpha p2; r2 = r1 - alpha q; r2'r2   (CG_solver.m:31-35)
-        launch_xr32(c, n3, x, ra, pa, M.cg_q32.as<float>(), scal, cur, dot_out(M, SC_RR), M.dot_blocks);
+        update_jacobi(0, cur);     // x += alpha p2; r2 = r1 - alpha q; |r2|; next Jacobi step
         c.mark(PK_CG_ITER, true);
         GMGS_CUDA(cudaMemcpyAsync(M.scal_host + SC_RR, scal + SC_RR, sizeof(double), cudaMemcpyDeviceToHost,
                                   c.stream));

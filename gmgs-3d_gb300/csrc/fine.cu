@@ -1,10 +1,12 @@
-// Tiled FP32 operator kernels of the mixed-precision path.
+// Streaming FP32 operator kernels of the mixed-precision path.
 //
-// One CTA owns a 32 x 8 column of nodes (y fastest) and streams it through z
-// with a three-plane ring of the input field plus a one-node halo in shared
-// memory; the field is computed while staging from the kernel's inputs (the
+// One CTA owns a 32 x 8 column of nodes (y fastest) and walks it through z
+// with a three-plane ring of the input field (plus a one-node halo) in shared
+// memory.  The field is formed while staging from the kernel's inputs (the
 // Jacobi step omega*D^-1 r, or the CG direction z + beta p), so no
-// intermediate vector goes through HBM.
+// intermediate vector goes through HBM.  The plane two steps ahead and the
+// per-node data of the next plane are loaded into registers while the current
+// plane is computed, so global loads overlap the stencil arithmetic.
 //
 // Interior nodes (all 8 surrounding elements carry the level's uniform
 // matrix) use the assembled 27-point stencil in second-difference form
@@ -18,6 +20,12 @@
 // translations), with per-element matrices where the level stores them
 // (the reference's AtX states 0/1/2, src/kernel/AtX.m:1-58).
 // Fixed DOF rows are zeroed (AtX.m:57).
+//
+// FP64 is used only where the outer CG keeps its state: x and r are FP64
+// vectors updated with FP32-formed increments; dot products sum FP32 products
+// with per-thread compensated (Kahan) FP32 sums and FP64 across threads and
+// blocks.  (GB300 runs FP64 and FP32<->FP64 conversions at 2 per clock per
+// SM, 1/64 of its FP32 rate.)
 #include "fine.cuh"
 
 namespace gmgs {
@@ -25,6 +33,8 @@ namespace gmgs {
 constexpr int TY = 32, TX = 8;
 constexpr int HY = TY + 2, HX = TX + 2;
 constexpr int NT = TY * TX;
+constexpr int PLANE = HY * HX;          // 340 points
+constexpr int NHALO = PLANE - NT;       // 84 halo points per plane
 
 // displacement component a (0 = x, 1 = y, 2 = z) of stencil offset k = (dz+1)*9 + (dx+1)*3 + (dy+1)
 __host__ __device__ constexpr int off_y(int k) { return k % 3 - 1; }
@@ -58,11 +68,18 @@ void make_stencil(const double* ke_rows, Coef32& cf) {
 }
 
 // ---------------------------------------------------------------------------
-// device helpers
+// reductions
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ bool in_halo_grid(const Grid& g, int iy, int ix, int iz) {
-    return iy >= -1 && ix >= -1 && iz >= -1 && iy <= g.ny + 1 && ix <= g.nx + 1 && iz <= g.nz + 1;
-}
+struct Kahan {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float v) {
+        const float y = v - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
 
 __device__ __forceinline__ double block_sum_d(double v, double* sh) {
 #pragma unroll
@@ -73,7 +90,7 @@ __device__ __forceinline__ double block_sum_d(double v, double* sh) {
     __syncthreads();
     v = 0;
     if (w == 0) {
-        v = l < NT / 32 ? sh[l] : 0.0;
+        v = l < (int)((blockDim.x * blockDim.y) >> 5) ? sh[l] : 0.0;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     }
@@ -85,6 +102,7 @@ __device__ __forceinline__ double block_sum_d(double v, double* sh) {
 __device__ void grid_dot_finish(double v, const DotOut& d, double* sh) {
     __shared__ bool last;
     v = block_sum_d(v, sh);
+    const int nthr = blockDim.x * blockDim.y;
     const int tid = threadIdx.x + threadIdx.y * blockDim.x;
     const unsigned nb = gridDim.x * gridDim.y * gridDim.z;
     const unsigned b = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
@@ -97,7 +115,7 @@ __device__ void grid_dot_finish(double v, const DotOut& d, double* sh) {
     if (last) {
         __threadfence();
         double t = 0;
-        for (unsigned i = tid; i < nb; i += NT) t += ((volatile double*)d.partials)[i];
+        for (unsigned i = tid; i < nb; i += nthr) t += ((volatile double*)d.partials)[i];
         t = block_sum_d(t, sh);
         if (tid == 0) {
             *d.out = t;
@@ -107,217 +125,261 @@ __device__ void grid_dot_finish(double v, const DotOut& d, double* sh) {
 }
 
 // ---------------------------------------------------------------------------
-// the fused streaming kernel
-//
-// A CTA of 32 x 8 threads owns a 32 x 8 column of nodes and walks it through
-// ZC planes in z.  Shared memory holds a ring of three (32+2) x (8+2) planes
-// of the input field; the plane two steps ahead is loaded (and transformed)
-// into registers while the current plane is computed, so global loads
-// overlap the stencil arithmetic.
+// stencil arithmetic on the shared-memory ring
 // ---------------------------------------------------------------------------
-constexpr int PLANE = HY * HX;                 // 340 points
-constexpr int PPT = (PLANE + NT - 1) / NT;     // points per thread and plane
-
-struct PlaneRegs {
-    float v[PPT][3];
-};
-
-struct Scalars {
-    float beta;      // FM_CG_DIRECTION
-    double alpha;    // FM_CG_UPDATE_JACOBI
-};
-
-template <int MODE>
-__device__ __forceinline__ void fetch_plane(const Grid& g, const FineArgs& a, const Scalars& sc, int y0, int x0, int iz,
-                                            int tid, PlaneRegs& pr) {
-    const int64_t S = g.slots;
-#pragma unroll
-    for (int k = 0; k < PPT; ++k) {
-        const int t = tid + k * NT;
-        const int ly = t % HY, lx = t / HY;
-        const int iy = y0 - 1 + ly, ix = x0 - 1 + lx;
-        float v[3] = {0.f, 0.f, 0.f};
-        if (t < PLANE && in_halo_grid(g, iy, ix, iz)) {
-            const int64_t s = g.slot(iy, ix, iz);
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                const int64_t i = s + c * S;
-                if (MODE == FM_PLAIN) {
-                    v[c] = a.v[i];
-                } else if (MODE == FM_VCYCLE_DOWN) {
-                    v[c] = a.r32[i] * a.wdinv[i];
-                } else if (MODE == FM_CG_UPDATE_JACOBI) {
-                    const double rm = a.first ? a.r64[i] : a.r64[i] - sc.alpha * (double)a.q32[i];
-                    v[c] = (float)rm * a.wdinv[i];
-                } else {   // FM_CG_DIRECTION
-                    v[c] = a.first ? a.z32[i] : fmaf(sc.beta, a.pold[i], a.z32[i]);
-                }
-            }
-        }
-#pragma unroll
-        for (int c = 0; c < 3; ++c) pr.v[k][c] = v[c];
-    }
-}
-
-__device__ __forceinline__ void store_plane(float* __restrict__ ring, int tid, const PlaneRegs& pr) {
-#pragma unroll
-    for (int k = 0; k < PPT; ++k) {
-        const int t = tid + k * NT;
-        if (t < PLANE) {
-#pragma unroll
-            for (int c = 0; c < 3; ++c) ring[c * PLANE + t] = pr.v[k][c];
-        }
-    }
-}
-
-// interior node, second-difference form; P[0..2] = planes z-1, z, z+1, p = in-plane index
-__device__ __forceinline__ void interior_s(const Coef32& cf, const float* const P[3], int p, float acc[3]) {
-    const float c[3] = {P[1][p], P[1][p + PLANE], P[1][p + 2 * PLANE]};
-    acc[0] = acc[1] = acc[2] = 0.f;
+// interior node, second-difference form; P0, P1, P2 = planes z-1, z, z+1
+__device__ __forceinline__ void interior_s(const Coef32& cf, const float* __restrict__ P0, const float* __restrict__ P1,
+                                           const float* __restrict__ P2, int p, float& y0, float& y1, float& y2) {
+    const float c0 = P1[p], c1 = P1[p + PLANE], c2 = P1[p + 2 * PLANE];
+    float acc[3] = {0.f, 0.f, 0.f};
 #pragma unroll
     for (int k = 14; k < 27; ++k) {
         const int o = off_y(k) + off_x(k) * HY;
-        const float* up = P[1 + off_z(k)];
-        const float* dn = P[1 - off_z(k)];
+        const float* up = off_z(k) > 0 ? P2 : (off_z(k) < 0 ? P0 : P1);
+        const float* dn = off_z(k) > 0 ? P0 : (off_z(k) < 0 ? P2 : P1);
         float d[3];
-#pragma unroll
-        for (int b = 0; b < 3; ++b) d[b] = (up[p + o + b * PLANE] - c[b]) + (dn[p - o + b * PLANE] - c[b]);
+        d[0] = (up[p + o] - c0) + (dn[p - o] - c0);
+        d[1] = (up[p + o + PLANE] - c1) + (dn[p - o + PLANE] - c1);
+        d[2] = (up[p + o + 2 * PLANE] - c2) + (dn[p - o + 2 * PLANE] - c2);
 #pragma unroll
         for (int a = 0; a < 3; ++a)
 #pragma unroll
             for (int b = 0; b < 3; ++b)
                 if (s_nonzero(k, a, b)) acc[a] = fmaf(cf.S[k * 9 + 3 * a + b], d[b], acc[a]);
     }
+    y0 = acc[0]; y1 = acc[1]; y2 = acc[2];
 }
 
-template <int CI>
-__device__ __forceinline__ void elem_rows_s(const float* __restrict__ K, float s, const float* const P[3], int p, int A,
-                                            int B, int C, const float c[3], float acc[3]) {
+// rows of one element (node at corner CI of the element with origin offset
+// (A, B, C)), first-difference form, coefficients K (row = output DOF) * s
+template <int A, int B, int C, bool PARAM>
+__device__ __forceinline__ void elem_rows(const Coef32& cf, const float* __restrict__ Kg, float s,
+                                          const float* __restrict__ P0, const float* __restrict__ P1,
+                                          const float* __restrict__ P2, int p, float c0, float c1, float c2,
+                                          float& y0, float& y1, float& y2) {
+    constexpr int CI = corner_of(A, B, C);
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
         if (j == CI) continue;
         const int dy = corner_y(j) - A, dx = corner_x(j) - B, dz = corner_z(j) - C;
-        const float* pl = P[1 + dz];
+        const float* pl = dz > 0 ? P2 : (dz < 0 ? P0 : P1);
         const int q = p + dy + dx * HY;
-        const float d0 = pl[q] - c[0], d1 = pl[q + PLANE] - c[1], d2 = pl[q + 2 * PLANE] - c[2];
+        const float d0 = pl[q] - c0, d1 = pl[q + PLANE] - c1, d2 = pl[q + 2 * PLANE] - c2;
+        float t[3];
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
             const int r = (3 * CI + a) * 24 + 3 * j;
-            float t = K[r] * d0;
-            t = fmaf(K[r + 1], d1, t);
-            t = fmaf(K[r + 2], d2, t);
-            acc[a] = fmaf(s, t, acc[a]);
+            if (PARAM) {
+                t[a] = fmaf(cf.K[r + 2], d2, fmaf(cf.K[r + 1], d1, cf.K[r] * d0));
+            } else {
+                t[a] = fmaf(Kg[r + 2], d2, fmaf(Kg[r + 1], d1, Kg[r] * d0));
+            }
         }
+        y0 = fmaf(s, t[0], y0);
+        y1 = fmaf(s, t[1], y1);
+        y2 = fmaf(s, t[2], y2);
     }
 }
 
 template <int E>
-__device__ __forceinline__ void boundary_elem_s(const FineLevel& L, const Coef32& cf, const float* const P[3], int p,
-                                                int64_t n, const float c[3], float acc[3]) {
+__device__ __forceinline__ void boundary_elem(const FineLevel& L, const Coef32& cf, uint32_t e8, int n,
+                                              const float* __restrict__ P0, const float* __restrict__ P1,
+                                              const float* __restrict__ P2, int p, float c0, float c1, float c2,
+                                              float& y0, float& y1, float& y2) {
     constexpr int A = E & 1, B = (E >> 1) & 1, C = E >> 2;
-    constexpr int CI = corner_of(A, B, C);
-    const int64_t es = n - A - B * L.g.sx() - C * L.g.sz();
-    if (!L.emask[es]) return;
-    const int t = L.etype ? L.etype[es] : 0;
-    if (t > 0) {
-        elem_rows_s<CI>(L.Ks + (int64_t)(t - 1) * KE, 1.0f, P, p, A, B, C, c, acc);
-    } else {
-        const float s = L.escale ? L.kscale * L.escale[es] : L.kscale;
-        elem_rows_s<CI>(cf.K, s, P, p, A, B, C, c, acc);
+    if (!((e8 >> E) & 1u)) return;
+    const int es = n - A - B * L.g.py - C * L.g.py * L.g.px;
+    float s = L.kscale;
+    if (L.etype) {
+        const int t = L.etype[es];
+        if (t > 0) {
+            elem_rows<A, B, C, false>(cf, L.Ks + (int64_t)(t - 1) * KE, 1.f, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);
+            return;
+        }
+    }
+    if (L.escale) s *= L.escale[es];
+    elem_rows<A, B, C, true>(cf, nullptr, s, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);
+}
+
+__device__ __forceinline__ void boundary_s(const FineLevel& L, const Coef32& cf, uint32_t e8, int n,
+                                           const float* __restrict__ P0, const float* __restrict__ P1,
+                                           const float* __restrict__ P2, int p, float& y0, float& y1, float& y2) {
+    const float c0 = P1[p], c1 = P1[p + PLANE], c2 = P1[p + 2 * PLANE];
+    y0 = y1 = y2 = 0.f;
+    boundary_elem<0>(L, cf, e8, n, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);
+    boundary_elem<1>(L, cf, e8, n, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);
+    boundary_elem<2>(L, cf, e8, n, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);
+    boundary_elem<3>(L, cf, e8, n, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);
+    boundary_elem<4>(L, cf, e8, n, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);
+    boundary_elem<5>(L, cf, e8, n, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);
+    boundary_elem<6>(L, cf, e8, n, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);
+    boundary_elem<7>(L, cf, e8, n, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);
+}
+
+// ---------------------------------------------------------------------------
+// the fused streaming kernel
+// ---------------------------------------------------------------------------
+// input field at one point (3 components) from the kernel's inputs
+template <int MODE>
+__device__ __forceinline__ void field_at(const FineArgs& a, int S, int s, float beta, float alpha, float v[3]) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const int i = s + c * S;
+        if (MODE == FM_PLAIN) {
+            v[c] = a.v[i];
+        } else if (MODE == FM_VCYCLE_DOWN) {
+            v[c] = a.r32[i] * a.wdinv[i];
+        } else if (MODE == FM_CG_UPDATE_JACOBI) {
+            const float rm = a.first ? a.r32[i] : fmaf(-alpha, a.q32[i], a.r32[i]);
+            v[c] = rm * a.wdinv[i];
+        } else {   // FM_CG_DIRECTION
+            v[c] = a.first ? a.z32[i] : fmaf(beta, a.pold[i], a.z32[i]);
+        }
     }
 }
 
-__device__ __noinline__ void boundary_s(const FineLevel& L, const Coef32& cf, const float* const P[3], int p, int64_t n,
-                                        float acc[3]) {
-    const float c[3] = {P[1][p], P[1][p + PLANE], P[1][p + 2 * PLANE]};
-    acc[0] = acc[1] = acc[2] = 0.f;
-    boundary_elem_s<0>(L, cf, P, p, n, c, acc);
-    boundary_elem_s<1>(L, cf, P, p, n, c, acc);
-    boundary_elem_s<2>(L, cf, P, p, n, c, acc);
-    boundary_elem_s<3>(L, cf, P, p, n, c, acc);
-    boundary_elem_s<4>(L, cf, P, p, n, c, acc);
-    boundary_elem_s<5>(L, cf, P, p, n, c, acc);
-    boundary_elem_s<6>(L, cf, P, p, n, c, acc);
-    boundary_elem_s<7>(L, cf, P, p, n, c, acc);
+// per-node data the epilogue needs, prefetched one plane ahead
+struct NodeData {
+    uint32_t f = 0, e8 = 0;
+    float r[3];       // FM_VCYCLE_DOWN: r;  FM_CG_UPDATE_JACOBI: r32
+    float q[3];       // FM_CG_UPDATE_JACOBI
+    float pp[3];      // FM_CG_UPDATE_JACOBI: p
+    float dx[3];      // FM_CG_UPDATE_JACOBI: pending dx
+    double r64[3];    // FM_CG_UPDATE_JACOBI
+};
+
+template <int MODE>
+__device__ __forceinline__ void node_fetch(const FineLevel& L, const FineArgs& a, int S, int n, NodeData& d) {
+    d.f = L.nflag[n];
+    d.e8 = L.emask8[n];
+    if (!(d.f & NF_SOLID)) return;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const int i = n + c * S;
+        if (MODE == FM_VCYCLE_DOWN) d.r[c] = a.r32[i];
+        if (MODE == FM_CG_UPDATE_JACOBI) {
+            d.r[c] = a.r32[i];
+            d.r64[c] = a.r64[i];
+            if (!a.first) {
+                d.q[c] = a.q32[i];
+                d.pp[c] = a.pold[i];
+                d.dx[c] = a.dxp[i];
+            }
+        }
+    }
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(NT, 3) k_fine(FineLevel L, const __grid_constant__ Coef32 cf, FineArgs a, int zc) {
+__global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? 2 : 3) k_fine(FineLevel L, const __grid_constant__ Coef32 cf, FineArgs a, int zc) {
     __shared__ float ring[3][3 * PLANE];
     __shared__ double sh[32];
     const Grid& g = L.g;
-    const int64_t S = g.slots;
+    const int S = (int)g.slots;
+    const int sz = g.py * g.px;
     const int y0 = blockIdx.x * TY, x0 = blockIdx.y * TX;
     const int zb = blockIdx.z * zc;
     const int ze = min(zb + zc, g.nz + 1);        // node planes [zb, ze)
-    const int tid = threadIdx.x + threadIdx.y * TY;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int tid = tx + ty * TY;
 
-    Scalars sc;
-    sc.beta = 0.f;
-    sc.alpha = 0.0;
-    if (MODE == FM_CG_DIRECTION && !a.first) sc.beta = (float)(a.scal[a.cur] / a.scal[a.cur ^ 1]);
-    if (MODE == FM_CG_UPDATE_JACOBI && !a.first) sc.alpha = a.scal[a.cur] / a.scal[2];
+    float beta = 0.f, alpha = 0.f;
+    if (MODE == FM_CG_DIRECTION && !a.first) beta = (float)(a.scal[a.cur] / a.scal[a.cur ^ 1]);
+    if (MODE == FM_CG_UPDATE_JACOBI && !a.first) alpha = (float)(a.scal[a.cur] / a.scal[2]);
 
-    PlaneRegs pr;
-    fetch_plane<MODE>(g, a, sc, y0, x0, zb - 1, tid, pr);
-    store_plane(ring[(zb - 1 + 3) % 3], tid, pr);
-    fetch_plane<MODE>(g, a, sc, y0, x0, zb, tid, pr);
-    store_plane(ring[zb % 3], tid, pr);
-    fetch_plane<MODE>(g, a, sc, y0, x0, zb + 1, tid, pr);
+    // this thread's centre point and (for tid < NHALO) one halo point of every plane
+    const int cy = y0 + tx, cx = x0 + ty;
+    const int pc = (tx + 1) + (ty + 1) * HY;
+    const bool ccol = cy <= g.ny + 1 && cx <= g.nx + 1;
+    const int cbase = (cx + 1) * g.py + (cy + 1) + sz;          // slot(cy, cx, iz) = cbase + iz * sz
+    int ph = 0, hbase = 0;
+    bool hcol = false;
+    if (tid < NHALO) {
+        int ly, lx;
+        if (tid < 2 * HX) { ly = (tid & 1) ? HY - 1 : 0; lx = tid >> 1; }
+        else { const int k = tid - 2 * HX; lx = (k & 1) ? HX - 1 : 0; ly = 1 + (k >> 1); }
+        ph = ly + lx * HY;
+        const int hy = y0 - 1 + ly, hx = x0 - 1 + lx;
+        hcol = hy >= -1 && hx >= -1 && hy <= g.ny + 1 && hx <= g.nx + 1;
+        hbase = (hx + 1) * g.py + (hy + 1) + sz;
+    }
+    auto fetch = [&](int iz, float vc[3], float vh[3]) {
+        vc[0] = vc[1] = vc[2] = 0.f;
+        vh[0] = vh[1] = vh[2] = 0.f;
+        const bool zok = iz >= -1 && iz <= g.nz + 1;
+        if (zok && ccol) field_at<MODE>(a, S, cbase + iz * sz, beta, alpha, vc);
+        if (zok && hcol) field_at<MODE>(a, S, hbase + iz * sz, beta, alpha, vh);
+    };
+    auto store = [&](float* r, const float vc[3], const float vh[3]) {
+        r[pc] = vc[0]; r[pc + PLANE] = vc[1]; r[pc + 2 * PLANE] = vc[2];
+        if (tid < NHALO) { r[ph] = vh[0]; r[ph + PLANE] = vh[1]; r[ph + 2 * PLANE] = vh[2]; }
+    };
 
-    const int iy = y0 + threadIdx.x, ix = x0 + threadIdx.y;
-    const bool own = iy <= g.ny && ix <= g.nx;
-    const int p = (threadIdx.x + 1) + (threadIdx.y + 1) * HY;
-    double dot = 0.0;
+    float vc[3], vh[3];
+    fetch(zb - 1, vc, vh);
+    store(ring[(zb + 2) % 3], vc, vh);
+    fetch(zb, vc, vh);
+    store(ring[zb % 3], vc, vh);
+    fetch(zb + 1, vc, vh);
+
+    const bool own = cy <= g.ny && cx <= g.nx;
+    NodeData nd;
+    if (own) node_fetch<MODE>(L, a, S, cbase + zb * sz, nd);
+    Kahan dot;
 #pragma unroll 1
     for (int iz = zb; iz < ze; ++iz) {
-        store_plane(ring[(iz + 1) % 3], tid, pr);
+        store(ring[(iz + 1) % 3], vc, vh);
         __syncthreads();
-        if (iz + 2 <= g.nz + 1) fetch_plane<MODE>(g, a, sc, y0, x0, iz + 2, tid, pr);
-        const float* const P[3] = {ring[(iz + 2) % 3], ring[iz % 3], ring[(iz + 1) % 3]};
-        if (own) {
-            const int64_t n = g.slot(iy, ix, iz);
-            const uint8_t f = L.nflag[n];
-            if (f & NF_SOLID) {
-                float y[3];
-                if (f & NF_INTERIOR) {
-                    interior_s(cf, P, p, y);
-                    y[0] *= L.kscale; y[1] *= L.kscale; y[2] *= L.kscale;
-                } else {
-                    boundary_s(L, cf, P, p, n, y);
-                }
-                if (f & NF_FIX_X) y[0] = 0.f;
-                if (f & NF_FIX_Y) y[1] = 0.f;
-                if (f & NF_FIX_Z) y[2] = 0.f;
+        if (iz + 2 <= g.nz + 1) fetch(iz + 2, vc, vh);
+        const NodeData cur = nd;
+        if (own && iz + 1 < ze) node_fetch<MODE>(L, a, S, cbase + (iz + 1) * sz, nd);
+        const float* P0 = ring[(iz + 2) % 3];
+        const float* P1 = ring[iz % 3];
+        const float* P2 = ring[(iz + 1) % 3];
+        if (own && (cur.f & NF_SOLID)) {
+            const int n = cbase + iz * sz;
+            float y[3];
+            if (cur.f & NF_INTERIOR) {
+                interior_s(cf, P0, P1, P2, pc, y[0], y[1], y[2]);
+                y[0] *= L.kscale; y[1] *= L.kscale; y[2] *= L.kscale;
+            } else {
+                boundary_s(L, cf, cur.e8, n, P0, P1, P2, pc, y[0], y[1], y[2]);
+            }
+            if (cur.f & NF_FIX_X) y[0] = 0.f;
+            if (cur.f & NF_FIX_Y) y[1] = 0.f;
+            if (cur.f & NF_FIX_Z) y[2] = 0.f;
 #pragma unroll
-                for (int b = 0; b < 3; ++b) {
-                    const int64_t i = n + b * S;
-                    const float v = P[1][p + b * PLANE];
-                    if (MODE == FM_PLAIN) {
-                        a.out32[i] = y[b];
-                    } else if (MODE == FM_VCYCLE_DOWN) {
-                        a.out32[i] = a.r32[i] - y[b];                    // r' = r - A (omega D^-1 r)
-                    } else if (MODE == FM_CG_UPDATE_JACOBI) {
-                        // previous iteration's update x += alpha p, r -= alpha q (CG_solver.m:32-33),
-                        // then this iteration's Jacobi step (CG_solver.m:18-19), its dx kept pending
-                        const double rm = a.first ? a.r64[i] : a.r64[i] - sc.alpha * (double)a.q32[i];
-                        if (!a.first) a.x64[i] = (a.x64[i] + (double)a.dxp[i]) + sc.alpha * (double)a.pold[i];
-                        a.dxp[i] = v;
-                        const double rn = rm - (double)y[b];
-                        a.r64out[i] = rn;
-                        a.r32out[i] = (float)rn;
-                        dot += rm * rm;
-                    } else {
-                        a.pout[i] = v;
-                        a.out32[i] = y[b];                               // q = A p
-                        dot += (double)v * (double)y[b];
+            for (int b = 0; b < 3; ++b) {
+                const int i = n + b * S;
+                const float v = P1[pc + b * PLANE];
+                if (MODE == FM_PLAIN) {
+                    a.out32[i] = y[b];
+                } else if (MODE == FM_VCYCLE_DOWN) {
+                    a.out32[i] = cur.r[b] - y[b];                        // r' = r - A (omega D^-1 r)
+                } else if (MODE == FM_CG_UPDATE_JACOBI) {
+                    // previous iteration's update x += alpha p, r -= alpha q (CG_solver.m:32-33),
+                    // then this iteration's Jacobi step (CG_solver.m:18-19) with its dx kept pending
+                    float rinc = y[b];
+                    float rm32 = cur.r[b];
+                    if (!a.first) {
+                        a.x64[i] += (double)(cur.dx[b] + alpha * cur.pp[b]);
+                        rinc = fmaf(alpha, cur.q[b], rinc);
+                        rm32 = fmaf(-alpha, cur.q[b], rm32);
                     }
+                    const double rn = cur.r64[b] - (double)rinc;
+                    a.r64[i] = rn;
+                    a.r32out[i] = (float)rn;
+                    a.dxp[i] = v;
+                    dot.add(rm32 * rm32);
+                } else {
+                    a.pout[i] = v;
+                    a.out32[i] = y[b];                                   // q = A p
+                    dot.add(v * y[b]);
                 }
             }
         }
         __syncthreads();
     }
-    if (MODE == FM_CG_DIRECTION || MODE == FM_CG_UPDATE_JACOBI) grid_dot_finish(dot, a.dot, sh);
+    if (MODE == FM_CG_DIRECTION || MODE == FM_CG_UPDATE_JACOBI) grid_dot_finish(dot.value(), a.dot, sh);
 }
 
 static int pick_zc(const Grid& g, const Ctx& c) {
@@ -349,123 +411,71 @@ template void launch_fine<FM_CG_DIRECTION>(Ctx&, const FineLevel&, const Coef32&
 // ---------------------------------------------------------------------------
 // V-cycle up-sweep in FP32 with omega D^-1 precomputed (Vcycle.m:29-32):
 // x_f = (w r + P x_c) + w r', optionally the finest-level fixed DOFs zeroed
-// and the CG dot r64 . x_f accumulated (CG_solver.m:26).
+// and the CG dot r . x_f accumulated (CG_solver.m:26).
 // ---------------------------------------------------------------------------
 template <bool DOT>
 __global__ void __launch_bounds__(256) k_up32(Grid gf, Grid gc, const uint8_t* __restrict__ nflag,
                                               const float* __restrict__ wdinv, const float* __restrict__ r,
                                               const float* __restrict__ rp, const float* __restrict__ xc,
-                                              float* __restrict__ xf, int zero_fixed, const double* __restrict__ r64,
-                                              DotOut dout) {
+                                              float* __restrict__ xf, int zero_fixed, DotOut dout) {
     __shared__ double sh[32];
     const int iy = blockIdx.x * blockDim.x + threadIdx.x;
     const int ix = blockIdx.y * blockDim.y + threadIdx.y;
     const int iz = blockIdx.z;
-    double dot = 0.0;
+    Kahan dot;
     if (iy <= gf.ny && ix <= gf.nx) {
-        const int64_t fs = gf.slot(iy, ix, iz);
+        const int fs = (int)gf.slot(iy, ix, iz);
         const uint8_t fl = nflag[fs];
         if (fl & NF_SOLID) {
-            const int64_t Sf = gf.slots, Sc = gc.slots;
+            const int Sf = (int)gf.slots, Sc = (int)gc.slots;
             const int Iy = iy >> 1, Ix = ix >> 1, Iz = iz >> 1;
             const int oy = iy & 1, ox = ix & 1, oz = iz & 1;
-            const int64_t c0 = gc.slot(Iy, Ix, Iz);
-            const int64_t csx = gc.sx(), csz = gc.sz();
+            const int c0 = (int)gc.slot(Iy, Ix, Iz);
+            const int csx = gc.py, csz = gc.py * gc.px;
             const float w = (oy ? 0.5f : 1.f) * (ox ? 0.5f : 1.f) * (oz ? 0.5f : 1.f);
 #pragma unroll
             for (int comp = 0; comp < 3; ++comp) {
                 const float* x = xc + comp * Sc;
-                float v = 0.f;
-                for (int cz = 0; cz <= oz; ++cz)
-                    for (int b = 0; b <= ox; ++b)
-                        for (int a = 0; a <= oy; ++a) v += x[c0 + a + b * csx + cz * csz];
-                const int64_t i = fs + comp * Sf;
+                float v = x[c0];
+                if (oy) v += x[c0 + 1];
+                if (ox) {
+                    v += x[c0 + csx];
+                    if (oy) v += x[c0 + csx + 1];
+                }
+                if (oz) {
+                    v += x[c0 + csz];
+                    if (oy) v += x[c0 + csz + 1];
+                    if (ox) {
+                        v += x[c0 + csz + csx];
+                        if (oy) v += x[c0 + csz + csx + 1];
+                    }
+                }
+                const int i = fs + comp * Sf;
                 const float wd = wdinv[i];
-                float out = (wd * r[i] + w * v) + wd * rp[i];
+                const float ri = r[i];
+                float out = (wd * ri + w * v) + wd * rp[i];
                 if (zero_fixed && (fl & (NF_FIX_X << comp))) out = 0.f;
                 xf[i] = out;
-                if (DOT) dot += r64[i] * (double)out;
+                if (DOT) dot.add(ri * out);
             }
         }
     }
-    if (DOT) {
-        // reuse the tiled reduction (blockDim 32 x 8 = NT)
-        grid_dot_finish(dot, dout, sh);
-    }
+    if (DOT) grid_dot_finish(dot.value(), dout, sh);
 }
 
 void launch_up32(Ctx& c, const Grid& gf, const Grid& gc, const uint8_t* nflag, const float* wdinv, const float* r,
-                 const float* rp, const float* xc, float* xf, bool zero_fixed, const double* r64, const DotOut* dot) {
+                 const float* rp, const float* xc, float* xf, bool zero_fixed, const DotOut* dot) {
     dim3 blk(32, 8, 1);
     dim3 grid((gf.ny + 1 + 31) / 32, (gf.nx + 1 + 7) / 8, gf.nz + 1);
     if (dot) {
-        k_up32<true><<<grid, blk, 0, c.stream>>>(gf, gc, nflag, wdinv, r, rp, xc, xf, zero_fixed, r64, *dot);
+        k_up32<true><<<grid, blk, 0, c.stream>>>(gf, gc, nflag, wdinv, r, rp, xc, xf, zero_fixed, *dot);
     } else {
-        k_up32<false><<<grid, blk, 0, c.stream>>>(gf, gc, nflag, wdinv, r, rp, xc, xf, zero_fixed, nullptr, DotOut{});
+        k_up32<false><<<grid, blk, 0, c.stream>>>(gf, gc, nflag, wdinv, r, rp, xc, xf, zero_fixed, DotOut{});
     }
     GMGS_LAUNCHED(c);
 }
 
 int up32_grid_blocks(const Grid& gf) { return ((gf.ny + 1 + 31) / 32) * ((gf.nx + 1 + 7) / 8) * (gf.nz + 1); }
-
-// ---------------------------------------------------------------------------
-// CG update (CG_solver.m:31-35): x += alpha p, r -= alpha q, r.r
-// ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_xr32(int64_t n, double* __restrict__ x, double* __restrict__ r,
-                                              const float* __restrict__ p, const float* __restrict__ q,
-                                              const double* __restrict__ scal, int cur, DotOut dout) {
-    __shared__ double sh[32];
-    __shared__ bool last;
-    const double alpha = scal[cur] / scal[2];
-    double acc = 0.0;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        x[i] = x[i] + alpha * (double)p[i];
-        const double rn = r[i] - alpha * (double)q[i];
-        r[i] = rn;
-        acc += rn * rn;
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-    if (l == 0) sh[w] = acc;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        acc = l < (int)(blockDim.x >> 5) ? sh[l] : 0.0;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-    }
-    if (threadIdx.x == 0) {
-        dout.partials[blockIdx.x] = acc;
-        __threadfence();
-        last = atomicAdd(dout.ticket, 1u) == gridDim.x - 1;
-    }
-    __syncthreads();
-    if (last) {
-        __threadfence();
-        double t = 0;
-        for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) t += ((volatile double*)dout.partials)[i];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
-        __syncthreads();
-        if (l == 0) sh[w] = t;
-        __syncthreads();
-        if (threadIdx.x < 32) {
-            t = l < (int)(blockDim.x >> 5) ? sh[l] : 0.0;
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
-            if (threadIdx.x == 0) {
-                *dout.out = t;
-                *dout.ticket = 0;
-            }
-        }
-    }
-}
-
-void launch_xr32(Ctx& c, int64_t n, double* x, double* r, const float* p, const float* q, const double* scal, int cur,
-                 const DotOut& d, int blocks) {
-    k_xr32<<<blocks, 256, 0, c.stream>>>(n, x, r, p, q, scal, cur, d);
-    GMGS_LAUNCHED(c);
-}
 
 // omega / diag in FP32 (0 where the diagonal is 0)
 __global__ void k_wdinv(int64_t n, const double* __restrict__ d, double omega, float* __restrict__ w) {
@@ -475,6 +485,37 @@ __global__ void k_wdinv(int64_t n, const double* __restrict__ d, double omega, f
 void launch_wdinv(Ctx& c, int64_t n, const double* d, double omega, float* w) {
     const int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)c.num_sms * 16);
     k_wdinv<<<blocks, 256, 0, c.stream>>>(n, d, omega, w);
+    GMGS_LAUNCHED(c);
+}
+
+// per-node bit mask of the 8 surrounding solid elements, bit A + 2B + 4C for
+// the element whose origin is the node minus (A, B, C)
+__global__ void k_emask8(Grid g, const uint8_t* __restrict__ emask, uint8_t* __restrict__ e8) {
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < g.slots; s += (int64_t)gridDim.x * blockDim.x) {
+        const int iy = (int)(s % g.py) - 1;
+        const int64_t r = s / g.py;
+        const int ix = (int)(r % g.px) - 1, iz = (int)(r / g.px) - 1;
+        uint8_t m = 0;
+        if (iy >= 0 && ix >= 0 && iz >= 0 && iy <= g.ny && ix <= g.nx && iz <= g.nz)
+            for (int e = 0; e < 8; ++e)
+                if (emask[s - (e & 1) - ((e >> 1) & 1) * g.sx() - (e >> 2) * g.sz()]) m |= (uint8_t)(1u << e);
+        e8[s] = m;
+    }
+}
+void launch_emask8(Ctx& c, const Grid& g, const uint8_t* emask, uint8_t* e8) {
+    const int blocks = (int)std::min<int64_t>((g.slots + 255) / 256, (int64_t)c.num_sms * 16);
+    k_emask8<<<blocks, 256, 0, c.stream>>>(g, emask, e8);
+    GMGS_LAUNCHED(c);
+}
+
+// r32 = fl32(b) for the first Jacobi step
+__global__ void k_to_f32(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        b[i] = (float)a[i];
+}
+void launch_to_f32(Ctx& c, int64_t n, const double* a, float* b) {
+    const int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)c.num_sms * 16);
+    k_to_f32<<<blocks, 256, 0, c.stream>>>(n, a, b);
     GMGS_LAUNCHED(c);
 }
 

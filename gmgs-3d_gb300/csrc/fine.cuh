@@ -17,6 +17,7 @@ struct FineLevel {
     Grid g;
     const uint8_t* emask;
     const uint8_t* nflag;    // NF_INTERIOR: all 8 elements carry kscale * Ke0
+    const uint8_t* emask8;   // per node: bit A + 2B + 4C set when the element at node - (A, B, C) is solid
     const int32_t* etype;    // null: every solid element uses kscale * Ke0
     const float* Ks;         // per-element matrices (FP32), row = output DOF
     const float* escale;     // finest-level element scale or null
@@ -40,8 +41,8 @@ enum FineMode {
 
 struct FineArgs {
     const float* v = nullptr;        // FM_PLAIN input
-    const float* r32 = nullptr;      // FM_VCYCLE_DOWN input residual
-    const double* r64 = nullptr;     // FM_CG_JACOBI input residual (read on the halo)
+    const float* r32 = nullptr;      // FM_VCYCLE_DOWN / FM_CG_UPDATE_JACOBI residual in FP32 (read on the halo)
+    double* r64 = nullptr;           // FM_CG_UPDATE_JACOBI residual in FP64 (owned nodes, updated in place)
     const float* wdinv = nullptr;    // omega / diag (3 planes)
     const float* z32 = nullptr;      // FM_CG_DIRECTION preconditioned residual
     const float* pold = nullptr;     // previous direction (FM_CG_DIRECTION: p_{k-1}; FM_CG_UPDATE_JACOBI: p_k)
@@ -52,8 +53,7 @@ struct FineArgs {
     float* out32 = nullptr;          // y / r' / q
     float* pout = nullptr;           // new direction (must not alias pold)
     double* x64 = nullptr;           // solution (owned nodes, in place)
-    double* r64out = nullptr;        // updated residual (must not alias r64)
-    float* r32out = nullptr;         // FP32 copy of the updated residual
+    float* r32out = nullptr;         // FP32 copy of the updated residual (must not alias r32)
     DotOut dot;
 };
 
@@ -67,9 +67,9 @@ template <int MODE>
 void launch_fine(Ctx& c, const FineLevel& L, const Coef32& cf, const FineArgs& a);
 
 void launch_up32(Ctx& c, const Grid& gf, const Grid& gc, const uint8_t* nflag, const float* wdinv, const float* r,
-                 const float* rp, const float* xc, float* xf, bool zero_fixed, const double* r64, const DotOut* dot);
-void launch_xr32(Ctx& c, int64_t n, double* x, double* r, const float* p, const float* q, const double* scal, int cur,
-                 const DotOut& d, int blocks);
+                 const float* rp, const float* xc, float* xf, bool zero_fixed, const DotOut* dot);
 void launch_wdinv(Ctx& c, int64_t n, const double* d, double omega, float* w);
+void launch_emask8(Ctx& c, const Grid& g, const uint8_t* emask, uint8_t* e8);
+void launch_to_f32(Ctx& c, int64_t n, const double* a, float* b);
 
 }  // namespace gmgs

@@ -139,6 +139,7 @@ struct Level {
     // V-cycle work vectors (3 planes each), precision of the V-cycle
     DevBuf vr, vrp, vdx, vx, vy;
     DevBuf wdinv32;           // mixed path: omega / diag in FP32
+    DevBuf emask8;            // mixed path: per-node mask of the 8 surrounding solid elements
 };
 
 // Per-launch CUDA-event timing of selected kernels (diagnostics; off by default).

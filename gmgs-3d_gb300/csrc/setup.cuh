@@ -30,7 +30,7 @@ struct Model {
     // outer CG work vectors
     DevBuf cg_x, cg_r, cg_p, cg_dx, cg_q64, cg_y64, cg_z64;   // FP64 path
     DevBuf cg_q32, cg_y32, cg_z32, cg_r32;                     // mixed path
-    DevBuf cg_r64b, cg_pa, cg_pb, cg_dxp;                      // mixed path double buffers, pending dx
+    DevBuf cg_r32b, cg_pa, cg_pb, cg_dxp;                      // mixed path double buffers, pending dx
     Coef32 coef{};                                             // FP32 stencil + element matrix
     DevBuf scal;           // device scalars (see solver.cu)
     DevBuf dot_partials, dot_ticket;

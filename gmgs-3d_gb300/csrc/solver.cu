@@ -49,6 +49,8 @@ void alloc_work(Model& M) {
             } else {
                 if (lv.wdinv32.bytes < n3 * 4) lv.wdinv32 = dalloc(n3 * 4);
                 launch_wdinv(c, (int64_t)n3, lv.diag64.as<double>(), M.prm.omega, lv.wdinv32.as<float>());
+                if (lv.emask8.bytes < (size_t)lv.g.slots) lv.emask8 = dalloc(lv.g.slots);
+                launch_emask8(c, lv.g, lv.emask.as<uint8_t>(), lv.emask8.as<uint8_t>());
             }
         }
     }
@@ -56,7 +58,7 @@ void alloc_work(Model& M) {
     zalloc(c, M.cg_x, n3 * 8);
     zalloc(c, M.cg_r, n3 * 8);
     if (mixed) {
-        zalloc(c, M.cg_r64b, n3 * 8);
+        zalloc(c, M.cg_r32b, n3 * 4);
         zalloc(c, M.cg_pa, n3 * 4);
         zalloc(c, M.cg_pb, n3 * 4);
         zalloc(c, M.cg_q32, n3 * 4);
@@ -118,13 +120,13 @@ static void vcycle(Model& M, const T* r0, T* z) {
     c.mark(PK_VCYCLE, true);
 }
 
-static void vcycle32(Model& M, const float* r32, float* z, const double* r64, int dot_slot);
+static void vcycle32(Model& M, const float* r32, float* z, bool with_dot, int dot_slot);
 
 void vcycle_apply(Model& M, const double* r, double* z) {
     const int64_t n3 = 3 * M.levels[0].g.slots;
     if (M.prm.precision == GMGS_MIXED) {
         launch_copy<float, double>(M.ctx, n3, M.cg_r32.as<float>(), r);
-        vcycle32(M, M.cg_r32.as<float>(), M.cg_z32.as<float>(), nullptr, 0);
+        vcycle32(M, M.cg_r32.as<float>(), M.cg_z32.as<float>(), false, 0);
         launch_copy<double, float>(M.ctx, n3, z, M.cg_z32.as<float>());
     } else {
         vcycle<double>(M, r, z);
@@ -147,6 +149,7 @@ static FineLevel fine_level(const Level& lv) {
     f.g = lv.g;
     f.emask = lv.emask.as<uint8_t>();
     f.nflag = lv.nflag.as<uint8_t>();
+    f.emask8 = lv.emask8.as<uint8_t>();
     f.etype = lv.etype.as<int32_t>();
     f.Ks = lv.Ks32.as<float>();
     f.escale = lv.escale32.as<float>();
@@ -162,8 +165,8 @@ static DotOut dot_out(Model& M, int slot) {
     return d;
 }
 
-// z = V(r32); the level-1 up-sweep also accumulates r64 . z into scal[dot_slot]
-static void vcycle32(Model& M, const float* r32, float* z, const double* r64, int dot_slot) {
+// z = V(r32); the level-1 up-sweep also accumulates r32 . z into scal[dot_slot]
+static void vcycle32(Model& M, const float* r32, float* z, bool with_dot, int dot_slot) {
     Ctx& c = M.ctx;
     const int L = M.num_levels;
     c.mark(PK_VCYCLE, false);
@@ -189,7 +192,7 @@ static void vcycle32(Model& M, const float* r32, float* z, const double* r64, in
         const DotOut d = dot_out(M, dot_slot);
         launch_up32(c, lv.g, M.levels[l + 1].g, lv.nflag.as<uint8_t>(), lv.wdinv32.as<float>(),
                     l == 0 ? r32 : lv.vr.as<float>(), lv.vrp.as<float>(), M.levels[l + 1].vx.as<float>(),
-                    l == 0 ? z : lv.vx.as<float>(), l == 0, l == 0 ? r64 : nullptr, (l == 0 && r64) ? &d : nullptr);
+                    l == 0 ? z : lv.vx.as<float>(), l == 0, (l == 0 && with_dot) ? &d : nullptr);
     }
     c.mark(PK_VCYCLE, true);
 }
@@ -200,16 +203,20 @@ static int pcg_mixed(Model& M, const double* b, double* x, int32_t* iters_out, d
     const int64_t n3 = 3 * l0.g.slots;
     double* scal = M.scal.as<double>();
     const DotScratch ds = dots(M);
-    double* ra = M.cg_r.as<double>();
-    double* rb = M.cg_r64b.as<double>();
+    double* r64 = M.cg_r.as<double>();
+    float* r32a = M.cg_r32.as<float>();
+    float* r32b = M.cg_r32b.as<float>();
     float* pa = M.cg_pa.as<float>();
     float* pb = M.cg_pb.as<float>();
+    float* dxp = M.cg_dxp.as<float>();
+    float* q = M.cg_q32.as<float>();
     const FineLevel f0 = fine_level(l0);
 
     launch_dot<double, double>(c, ds, n3, b, b, scal + SC_BB);
     GMGS_CUDA(cudaMemcpyAsync(M.scal_host + SC_BB, scal + SC_BB, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     GMGS_CUDA(cudaMemsetAsync(x, 0, n3 * sizeof(double), c.stream));
-    GMGS_CUDA(cudaMemcpyAsync(ra, b, n3 * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
+    GMGS_CUDA(cudaMemcpyAsync(r64, b, n3 * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));   // r = b - A*0
+    launch_to_f32(c, n3, b, r32a);
     GMGS_CUDA(cudaStreamSynchronize(c.stream));
     const double normB = std::sqrt(M.scal_host[SC_BB]);
     if (normB == 0.0) {
@@ -220,26 +227,24 @@ static int pcg_mixed(Model& M, const double* b, double* x, int32_t* iters_out, d
         return GMGS_OK;
     }
     if (!std::isfinite(normB)) throw Error(GMGS_ERR_NONFINITE, "non-finite load vector");
-    const double jbytes = (double)l0.n_node * 3 * (8 + 4 + 4 + 8 + 4 + 4 + 8 + 8 + 4 + 4) + (double)l0.n_elem;
-    const double pbytes = (double)l0.n_node * 3 * (4 + 4 + 4 + 4) + (double)l0.n_elem;
-    float* dxp = M.cg_dxp.as<float>();
-    float* q = M.cg_q32.as<float>();
-    float* r32 = M.cg_r32.as<float>();
+    // algorithmic bytes per node: r64 rw, r32 read + write, q, p, wdinv, x rw, dxp rw
+    const double jbytes = (double)l0.n_node * 3 * (16 + 8 + 4 + 4 + 4 + 16 + 8) + 2.0 * (double)l0.n_node;
+    const double pbytes = (double)l0.n_node * 3 * (4 + 4 + 4 + 4) + 2.0 * (double)l0.n_node;
 
-    // Fused kernel F: the previous iteration's update (x += alpha p, r -= alpha q,
+    // Fused kernel: the previous iteration's update (x += alpha p, r -= alpha q,
     // |r|^2 for its convergence test) followed by this iteration's Jacobi step,
     // whose dx stays pending until the next update, so x is always the
     // reference's x at the end of the last completed iteration.
     auto update_jacobi = [&](int first, int cur) {
         FineArgs a;
-        a.r64 = ra;
+        a.r32 = r32a;
+        a.r64 = r64;
         a.q32 = q;
         a.pold = pa;
         a.wdinv = l0.wdinv32.as<float>();
         a.x64 = x;
         a.dxp = dxp;
-        a.r64out = rb;
-        a.r32out = r32;
+        a.r32out = r32b;
         a.scal = scal;
         a.cur = cur;
         a.first = first;
@@ -247,7 +252,7 @@ static int pcg_mixed(Model& M, const double* b, double* x, int32_t* iters_out, d
         c.mark(PK_FINE_MATVEC, false);
         launch_fine<FM_CG_UPDATE_JACOBI>(c, f0, M.coef, a);
         c.mark(PK_FINE_MATVEC, true, jbytes);
-        std::swap(ra, rb);
+        std::swap(r32a, r32b);
     };
 
     const auto t0 = std::chrono::steady_clock::now();
@@ -259,7 +264,7 @@ static int pcg_mixed(Model& M, const double* b, double* x, int32_t* iters_out, d
         c.mark(PK_CG_ITER, false);
         ++its;
         const int cur = its & 1;
-        vcycle32(M, r32, M.cg_z32.as<float>(), ra, cur);     // z2 = PtV(r1), r1'z2   (CG_solver.m:21,26)
+        vcycle32(M, r32a, M.cg_z32.as<float>(), true, cur);     // z2 = PtV(r1), r1'z2   (CG_solver.m:21,26)
         {   // p2 = z2 + beta p1; q = A p2; p2'q   (CG_solver.m:23-31)
             FineArgs a;
             a.z32 = M.cg_z32.as<float>();
@@ -301,9 +306,6 @@ static int pcg_mixed(Model& M, const double* b, double* x, int32_t* iters_out, d
         }
         ++nhist;
     }
-    // keep the residual in the primary buffer for callers that read it
-    if (ra != M.cg_r.as<double>())
-        GMGS_CUDA(cudaMemcpyAsync(M.cg_r.p, ra, n3 * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
     if (status == GMGS_ERR_MAX_ITERATIONS && M.prm.verbose) std::printf("Exceed the maximum iterate numbers\n");
     if (iters_out) *iters_out = its;
     if (relres_out) *relres_out = resnorm;

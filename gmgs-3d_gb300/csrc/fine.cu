@@ -24,8 +24,8 @@
 // FP64 is used only where the outer CG keeps its state: x and r are FP64
 // vectors updated with FP32-formed increments; dot products sum FP32 products
 // with per-thread compensated (Kahan) FP32 sums and FP64 across threads and
-// blocks.  (GB300 runs FP64 and FP32<->FP64 conversions at 2 per clock per
-// SM, 1/64 of its FP32 rate.)
+// blocks.  (GB300 issues FP64 arithmetic at 2 operations per clock per SM,
+// 1/64 of its FP32 rate, and the FP32<->FP64 conversions use the same pipe.)
 #include "fine.cuh"
 
 namespace gmgs {

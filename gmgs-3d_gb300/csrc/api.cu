@@ -387,6 +387,62 @@ int gmgs_apply_preconditioner(gmgs_handle* h, const double* r, double* z) {
     });
 }
 
+int gmgs_apply_operator_dev(gmgs_handle* h, int32_t level, const double* x, double* y) {
+    return guarded(h, [&]() -> int {
+        if (!h || !x || !y) fail(GMGS_ERR_INVALID_ARGUMENT, "NULL argument");
+        gmgs::Model& M = h->M;
+        if (level < 1 || level > M.num_levels) fail(GMGS_ERR_INVALID_ARGUMENT, "level out of range");
+        ensure_coarse(h);
+        gmgs::Level& lv = M.levels[level - 1];
+        const int64_t nn = lv.n_node, S = lv.g.slots;
+        gmgs::DevBuf xd = gmgs::dalloc(3 * S * sizeof(double)), yd = gmgs::dalloc(3 * S * sizeof(double));
+        GMGS_CUDA(cudaMemsetAsync(xd.p, 0, 3 * S * sizeof(double), M.ctx.stream));
+        gmgs::launch_compact_to_dense<double>(M.ctx, nn, S, lv.node_slot.as<int32_t>(), x, xd.as<double>());
+        gmgs::apply_operator_dense(M, level - 1, xd.as<double>(), yd.as<double>());
+        gmgs::launch_dense_to_compact<double>(M.ctx, nn, S, lv.node_slot.as<int32_t>(), yd.as<double>(), y);
+        GMGS_CUDA(cudaStreamSynchronize(M.ctx.stream));
+        return GMGS_OK;
+    });
+}
+
+int gmgs_apply_preconditioner_dev(gmgs_handle* h, const double* r, double* z) {
+    return guarded(h, [&]() -> int {
+        if (!h || !r || !z) fail(GMGS_ERR_INVALID_ARGUMENT, "NULL argument");
+        gmgs::Model& M = h->M;
+        ensure_coarse(h);
+        gmgs::Level& lv = M.levels[0];
+        const int64_t nn = lv.n_node, S = lv.g.slots;
+        gmgs::DevBuf xd = gmgs::dalloc(3 * S * sizeof(double)), yd = gmgs::dalloc(3 * S * sizeof(double));
+        GMGS_CUDA(cudaMemsetAsync(xd.p, 0, 3 * S * sizeof(double), M.ctx.stream));
+        GMGS_CUDA(cudaMemsetAsync(yd.p, 0, 3 * S * sizeof(double), M.ctx.stream));
+        gmgs::launch_compact_to_dense<double>(M.ctx, nn, S, lv.node_slot.as<int32_t>(), r, xd.as<double>());
+        gmgs::vcycle_apply_fp64(M, xd.as<double>(), yd.as<double>());
+        gmgs::launch_dense_to_compact<double>(M.ctx, nn, S, lv.node_slot.as<int32_t>(), yd.as<double>(), z);
+        GMGS_CUDA(cudaStreamSynchronize(M.ctx.stream));
+        return GMGS_OK;
+    });
+}
+
+int gmgs_dot_dev(gmgs_handle* h, const double* x, const double* y, int64_t n, double* result) {
+    return guarded(h, [&]() -> int {
+        if (!h || !x || !y || !result || n < 0) fail(GMGS_ERR_INVALID_ARGUMENT, "invalid argument");
+        gmgs::Model& M = h->M;
+        if (!M.dot_partials.p) {
+            M.dot_blocks = M.ctx.num_sms * 4;
+            M.dot_partials = gmgs::dalloc(M.dot_blocks * sizeof(double));
+            M.dot_ticket = gmgs::dalloc(sizeof(unsigned int));
+            GMGS_CUDA(cudaMemsetAsync(M.dot_ticket.p, 0, sizeof(unsigned int), M.ctx.stream));
+        }
+        if (!M.scal.p) M.scal = gmgs::dalloc(8 * sizeof(double));
+        const gmgs::DotScratch ds{M.dot_partials.as<double>(), M.dot_ticket.as<unsigned int>(), M.dot_blocks};
+        double* out = M.scal.as<double>() + 7;
+        gmgs::launch_dot<double, double>(M.ctx, ds, n, x, y, out);
+        GMGS_CUDA(cudaMemcpyAsync(result, out, sizeof(double), cudaMemcpyDeviceToHost, M.ctx.stream));
+        GMGS_CUDA(cudaStreamSynchronize(M.ctx.stream));
+        return GMGS_OK;
+    });
+}
+
 int gmgs_num_levels(const gmgs_handle* h, int32_t* out) {
     if (!h || !out) return GMGS_ERR_INVALID_ARGUMENT;
     *out = h->M.num_levels;

@@ -60,6 +60,9 @@ SIGNATURES = {
     "gmgs_grad_dev": (C.c_int, [_p, _p, _p]),
     "gmgs_apply_operator": (C.c_int, [_p, _i32, _dp, _dp]),
     "gmgs_apply_preconditioner": (C.c_int, [_p, _dp, _dp]),
+    "gmgs_apply_operator_dev": (C.c_int, [_p, _i32, _p, _p]),
+    "gmgs_apply_preconditioner_dev": (C.c_int, [_p, _p, _p]),
+    "gmgs_dot_dev": (C.c_int, [_p, _p, _p, _i64, _dp]),
     "gmgs_num_levels": (C.c_int, [_p, _i32p]),
     "gmgs_num_nodes": (C.c_int, [_p, _i32, _i64p]),
     "gmgs_num_elements": (C.c_int, [_p, _i32, _i64p]),

@@ -215,6 +215,19 @@ class Solver:
         self._check(self._lib.gmgs_apply_operator(self._h, level, _dptr(x), _dptr(y)))
         return y
 
+    def apply_operator_dev(self, x_ptr: int, y_ptr: int, level: int = 1):
+        """AtX on device buffers (compact interleaved float64 of the level's DOFs)."""
+        self._check(self._lib.gmgs_apply_operator_dev(self._h, level, C.c_void_p(x_ptr), C.c_void_p(y_ptr)))
+
+    def apply_preconditioner_dev(self, r_ptr: int, z_ptr: int):
+        self._check(self._lib.gmgs_apply_preconditioner_dev(self._h, C.c_void_p(r_ptr), C.c_void_p(z_ptr)))
+
+    def dot_dev(self, x_ptr: int, y_ptr: int, n: int) -> float:
+        """Deterministic FP64 inner product of two device vectors of n doubles."""
+        out = C.c_double()
+        self._check(self._lib.gmgs_dot_dev(self._h, C.c_void_p(x_ptr), C.c_void_p(y_ptr), n, C.byref(out)))
+        return out.value
+
     def apply_preconditioner(self, r):
         """Vcycle(r) on a compact interleaved finest-level vector."""
         r = np.ascontiguousarray(np.asarray(r, dtype=np.float64))

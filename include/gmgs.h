@@ -129,6 +129,14 @@ int gmgs_grad_dev(gmgs_handle* h, const double* ell_dev, double* dJdrho_dev);
  * (BuildingMeshHierarchy.m:101-118).  Available after the first solve. */
 int gmgs_apply_operator(gmgs_handle* h, int32_t level, const double* x, double* y);
 int gmgs_apply_preconditioner(gmgs_handle* h, const double* r, double* z);
+/* The same on device buffers (compact interleaved), on the handle's stream. */
+int gmgs_apply_operator_dev(gmgs_handle* h, int32_t level, const double* x_dev, double* y_dev);
+int gmgs_apply_preconditioner_dev(gmgs_handle* h, const double* r_dev, double* z_dev);
+/* r1'*z2-style inner product of CG_solver.m:26,31,35 on device vectors:
+ * deterministic FP64 reduction (fixed partition and summation order, so
+ * repeated calls give identical bits) using the handle's scratch memory.
+ * *result is written on the host after the handle's stream is synchronised. */
+int gmgs_dot_dev(gmgs_handle* h, const double* x_dev, const double* y_dev, int64_t n, double* result);
 
 /* Sizes */
 int gmgs_num_levels(const gmgs_handle* h, int32_t* out);

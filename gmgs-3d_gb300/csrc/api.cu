@@ -120,6 +120,11 @@ int solve_impl(gmgs_handle* h, double* U_host, double* U_dev, int32_t* iters, do
 
 }  // namespace
 
+namespace gmgs {
+// error message for entry points that run without a handle
+void set_thread_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace gmgs
+
 extern "C" {
 
 void gmgs_default_params(gmgs_params* p) {

@@ -29,6 +29,8 @@ ERR_STATE = 12
 FP64 = 0
 MIXED = 1
 
+DOT_NOALLOC_MAX_N = 536870912   # GMGS_DOT_NOALLOC_MAX_N
+
 # every function the header declares, with (restype, argtypes)
 _p = C.c_void_p
 _i32 = C.c_int32
@@ -63,6 +65,7 @@ SIGNATURES = {
     "gmgs_apply_operator_dev": (C.c_int, [_p, _i32, _p, _p]),
     "gmgs_apply_preconditioner_dev": (C.c_int, [_p, _p, _p]),
     "gmgs_dot_dev": (C.c_int, [_p, _p, _p, _i64, _dp]),
+    "gmgs_dot_dev_noalloc": (C.c_int, [_p, _p, _i64, _p, _p]),
     "gmgs_num_levels": (C.c_int, [_p, _i32p]),
     "gmgs_num_nodes": (C.c_int, [_p, _i32, _i64p]),
     "gmgs_num_elements": (C.c_int, [_p, _i32, _i64p]),

@@ -138,6 +138,28 @@ int gmgs_apply_preconditioner_dev(gmgs_handle* h, const double* r_dev, double* z
  * *result is written on the host after the handle's stream is synchronised. */
 int gmgs_dot_dev(gmgs_handle* h, const double* x_dev, const double* y_dev, int64_t n, double* result);
 
+/* Allocation-free variant of gmgs_dot_dev; no counterpart in the reference.
+ * For callers that cannot allocate device memory: hosts whose device memory
+ * belongs to their own allocator (a MATLAB MEX shim working on gpuArray
+ * buffers, a framework whose caching allocator must see every allocation) and
+ * code paths that cannot afford the implicit device synchronisation of
+ * cudaMalloc / cudaFree.  It needs no handle and calls no allocating routine.
+ * Computes the deterministic FP64 inner product of two device vectors of n
+ * doubles into the device scalar *result_dev, asynchronously on `stream`
+ * (a cudaStream_t; NULL = the legacy default stream).
+ * Scratch: a fixed 512 KiB static device array inside libgmgs (65,536 block
+ * partials and an arrival counter), held by every GPU that loads the library
+ * until the process exits.  n must not exceed GMGS_DOT_NOALLOC_MAX_N
+ * (65,536 blocks x 8,192 elements); longer vectors get
+ * GMGS_ERR_INVALID_ARGUMENT (use gmgs_dot_dev).  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress) with that device
+ * current, so make that first call before any stream capture.  All calls
+ * share the array and each clears the counter it needs before its kernel
+ * runs; calls that overlap on the GPU (several streams or host threads at
+ * once) race on the array and must be serialised by the caller. */
+#define GMGS_DOT_NOALLOC_MAX_N 536870912LL
+int gmgs_dot_dev_noalloc(const double* x_dev, const double* y_dev, int64_t n, double* result_dev, void* stream);
+
 /* Sizes */
 int gmgs_num_levels(const gmgs_handle* h, int32_t* out);
 int gmgs_num_nodes(const gmgs_handle* h, int32_t level, int64_t* out);

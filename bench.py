@@ -237,6 +237,14 @@ def run_gmgs(a):
     its = s.iterations
     relres = s.relres
     nl, mv_ms, mv_bytes = s.kernel_time(0)
+    phase_names = {1: "vcycle", 2: "cg_iteration", 3: "fine_update_jacobi", 4: "fine_vcycle_down",
+                   5: "fine_direction", 6: "fine_prolong_post", 7: "coarse_levels"}
+    breakdown = {}
+    for k, name in phase_names.items():
+        n_k, ms_k, b_k = s.kernel_time(k)
+        breakdown[name] = {"launches": n_k, "ms_per_solve": ms_k / a.steps,
+                           "ms_per_launch": ms_k / max(n_k, 1),
+                           "gbs": (b_k / (ms_k / 1e3) / 1e9) if (b_k and ms_k) else None}
     if ws > 1:
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -309,6 +317,7 @@ def run_gmgs(a):
                      "kernel": "finest-level K*x", "launches_timed": nl,
                      "ms_per_launch": mv_ms / max(nl, 1), "peak_source": peak_note},
         "gpu_launches": launches,
+        "breakdown": breakdown,
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
         "e2e": e2e,

@@ -143,7 +143,17 @@ struct Level {
 };
 
 // Per-launch CUDA-event timing of selected kernels (diagnostics; off by default).
-enum ProfKernel { PK_FINE_MATVEC = 0, PK_VCYCLE = 1, PK_CG_ITER = 2, PK_COUNT = 3 };
+enum ProfKernel {
+    PK_FINE_MATVEC = 0,   // every finest-level stencil launch
+    PK_VCYCLE = 1,        // whole V-cycles
+    PK_CG_ITER = 2,       // whole CG iterations
+    PK_UPDATE_JACOBI = 3, // finest fused CG update + Jacobi step
+    PK_VDOWN0 = 4,        // finest V-cycle down-sweep
+    PK_DIRECTION = 5,     // finest CG direction + q = A p
+    PK_UP0 = 6,           // finest prolongation + post-smooth + r.z
+    PK_COARSE = 7,        // everything on levels 2..L of a V-cycle
+    PK_COUNT = 8
+};
 
 struct ProfSlot {
     std::vector<cudaEvent_t> ev;   // start/stop pairs

@@ -178,11 +178,19 @@ static void vcycle32(Model& M, const float* r32, float* z, bool with_dot, int do
         a.wdinv = lv.wdinv32.as<float>();
         a.out32 = lv.vrp.as<float>();
         const double bytes = (double)lv.n_node * 3 * 12 + (double)lv.n_elem;
-        if (l == 0) c.mark(PK_FINE_MATVEC, false);
+        if (l == 0) {
+            c.mark(PK_FINE_MATVEC, false);
+            c.mark(PK_VDOWN0, false);
+        }
+        if (l == 1) c.mark(PK_COARSE, false);
         launch_fine<FM_VCYCLE_DOWN>(c, fine_level(lv), M.coef, a);
-        if (l == 0) c.mark(PK_FINE_MATVEC, true, bytes);
+        if (l == 0) {
+            c.mark(PK_FINE_MATVEC, true, bytes);
+            c.mark(PK_VDOWN0, true, bytes);
+        }
         launch_restrict<float>(c, lv.g, lc.g, lc.nflag.as<uint8_t>(), lv.vrp.as<float>(), lc.vr.as<float>());
     }
+    if (L == 2) c.mark(PK_COARSE, false);
     Level& lc = M.levels[L - 1];
     launch_gather<float>(c, M.nfree, M.free_idx.as<int32_t>(), lc.vr.as<float>(), M.cvec_in.as<double>());
     launch_gemv(c, M.nfree, M.kinv.as<double>(), M.cvec_in.as<double>(), M.cvec_out.as<double>());
@@ -190,9 +198,14 @@ static void vcycle32(Model& M, const float* r32, float* z, bool with_dot, int do
     for (int l = L - 2; l >= 0; --l) {
         Level& lv = M.levels[l];
         const DotOut d = dot_out(M, dot_slot);
+        if (l == 0) {
+            c.mark(PK_COARSE, true);
+            c.mark(PK_UP0, false);
+        }
         launch_up32(c, lv.g, M.levels[l + 1].g, lv.nflag.as<uint8_t>(), lv.wdinv32.as<float>(),
                     l == 0 ? r32 : lv.vr.as<float>(), lv.vrp.as<float>(), M.levels[l + 1].vx.as<float>(),
                     l == 0 ? z : lv.vx.as<float>(), l == 0, (l == 0 && with_dot) ? &d : nullptr);
+        if (l == 0) c.mark(PK_UP0, true, (double)lv.n_node * 3 * 20);
     }
     c.mark(PK_VCYCLE, true);
 }
@@ -250,8 +263,10 @@ static int pcg_mixed(Model& M, const double* b, double* x, int32_t* iters_out, d
         a.first = first;
         a.dot = dot_out(M, SC_RR);
         c.mark(PK_FINE_MATVEC, false);
+        c.mark(PK_UPDATE_JACOBI, false);
         launch_fine<FM_CG_UPDATE_JACOBI>(c, f0, M.coef, a);
         c.mark(PK_FINE_MATVEC, true, jbytes);
+        c.mark(PK_UPDATE_JACOBI, true, jbytes);
         std::swap(r32a, r32b);
     };
 
@@ -276,8 +291,10 @@ static int pcg_mixed(Model& M, const double* b, double* x, int32_t* iters_out, d
             a.out32 = q;
             a.dot = dot_out(M, SC_PQ);
             c.mark(PK_FINE_MATVEC, false);
+            c.mark(PK_DIRECTION, false);
             launch_fine<FM_CG_DIRECTION>(c, f0, M.coef, a);
             c.mark(PK_FINE_MATVEC, true, pbytes);
+            c.mark(PK_DIRECTION, true, pbytes);
             std::swap(pa, pb);
         }
         update_jacobi(0, cur);     // x += alpha p2; r2 = r1 - alpha q; |r2|; next Jacobi step

@@ -175,8 +175,10 @@ int gmgs_phase_times(const gmgs_handle* h, double out[4]);   /* ms: create, bc-s
 /* Kernel timing with CUDA events on the handle's stream (diagnostics).
  * gmgs_set_profiling(h, 1) clears the records and starts recording;
  * gmgs_kernel_time() sums them.  kernel: 0 = finest-level K*x launches,
- * 1 = whole V-cycles, 2 = whole CG iterations.  bytes: algorithmic bytes of
- * the recorded launches (kernel 0 only). */
+ * 1 = whole V-cycles, 2 = whole CG iterations, 3 = finest CG update + Jacobi,
+ * 4 = finest V-cycle down-sweep, 5 = finest CG direction + A p, 6 = finest
+ * prolongation + post-smooth, 7 = levels 2..L of the V-cycles.  bytes:
+ * algorithmic bytes of the recorded launches (0 for whole phases). */
 int gmgs_set_profiling(gmgs_handle* h, int32_t enable);
 int gmgs_kernel_time(gmgs_handle* h, int32_t kernel, int64_t* launches, double* total_ms, double* bytes);
 const char* gmgs_last_error(const gmgs_handle* h);

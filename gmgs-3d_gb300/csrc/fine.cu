@@ -115,7 +115,7 @@ __device__ void grid_dot_finish(double v, const DotOut& d, double* sh) {
     if (last) {
         __threadfence();
         double t = 0;
-        for (unsigned i = tid; i < nb; i += nthr) t += ((volatile double*)d.partials)[i];
+        for (unsigned i = tid; i < nb; i += nthr) t += __ldcg(d.partials + i);
         t = block_sum_d(t, sh);
         if (tid == 0) {
             *d.out = t;
@@ -238,21 +238,16 @@ __device__ __forceinline__ void field_at(const FineArgs& a, int S, int s, float 
     }
 }
 
-// per-node data the epilogue needs, prefetched one plane ahead
-struct NodeData {
-    uint32_t f = 0, e8 = 0;
+// per-node epilogue inputs, loaded before the stencil arithmetic of the plane
+struct EpiData {
     float r[3];       // FM_VCYCLE_DOWN: r;  FM_CG_UPDATE_JACOBI: r32
     float q[3];       // FM_CG_UPDATE_JACOBI
     float pp[3];      // FM_CG_UPDATE_JACOBI: p
-    float dx[3];      // FM_CG_UPDATE_JACOBI: pending dx
     double r64[3];    // FM_CG_UPDATE_JACOBI
 };
 
 template <int MODE>
-__device__ __forceinline__ void node_fetch(const FineLevel& L, const FineArgs& a, int S, int n, NodeData& d) {
-    d.f = L.nflag[n];
-    d.e8 = L.emask8[n];
-    if (!(d.f & NF_SOLID)) return;
+__device__ __forceinline__ void epi_fetch(const FineArgs& a, int S, int n, EpiData& d) {
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         const int i = n + c * S;
@@ -263,14 +258,13 @@ __device__ __forceinline__ void node_fetch(const FineLevel& L, const FineArgs& a
             if (!a.first) {
                 d.q[c] = a.q32[i];
                 d.pp[c] = a.pold[i];
-                d.dx[c] = a.dxp[i];
             }
         }
     }
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? 2 : 3) k_fine(FineLevel L, const __grid_constant__ Coef32 cf, FineArgs a, int zc) {
+__global__ void __launch_bounds__(NT, 3) k_fine(FineLevel L, const __grid_constant__ Coef32 cf, FineArgs a, int zc) {
     __shared__ float ring[3][3 * PLANE];
     __shared__ double sh[32];
     const Grid& g = L.g;
@@ -322,31 +316,39 @@ __global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? 2 : 3) k_fin
     fetch(zb + 1, vc, vh);
 
     const bool own = cy <= g.ny && cx <= g.nx;
-    NodeData nd;
-    if (own) node_fetch<MODE>(L, a, S, cbase + zb * sz, nd);
+    uint32_t f_next = 0, e8_next = 0;
+    if (own) {
+        f_next = L.nflag[cbase + zb * sz];
+        e8_next = L.emask8[cbase + zb * sz];
+    }
     Kahan dot;
 #pragma unroll 1
     for (int iz = zb; iz < ze; ++iz) {
         store(ring[(iz + 1) % 3], vc, vh);
         __syncthreads();
         if (iz + 2 <= g.nz + 1) fetch(iz + 2, vc, vh);
-        const NodeData cur = nd;
-        if (own && iz + 1 < ze) node_fetch<MODE>(L, a, S, cbase + (iz + 1) * sz, nd);
+        const uint32_t f = f_next, e8 = e8_next;
+        if (own && iz + 1 < ze) {
+            f_next = L.nflag[cbase + (iz + 1) * sz];
+            e8_next = L.emask8[cbase + (iz + 1) * sz];
+        }
         const float* P0 = ring[(iz + 2) % 3];
         const float* P1 = ring[iz % 3];
         const float* P2 = ring[(iz + 1) % 3];
-        if (own && (cur.f & NF_SOLID)) {
+        if (own && (f & NF_SOLID)) {
             const int n = cbase + iz * sz;
+            EpiData ed;
+            epi_fetch<MODE>(a, S, n, ed);       // in flight during the stencil arithmetic
             float y[3];
-            if (cur.f & NF_INTERIOR) {
+            if (f & NF_INTERIOR) {
                 interior_s(cf, P0, P1, P2, pc, y[0], y[1], y[2]);
                 y[0] *= L.kscale; y[1] *= L.kscale; y[2] *= L.kscale;
             } else {
-                boundary_s(L, cf, cur.e8, n, P0, P1, P2, pc, y[0], y[1], y[2]);
+                boundary_s(L, cf, e8, n, P0, P1, P2, pc, y[0], y[1], y[2]);
             }
-            if (cur.f & NF_FIX_X) y[0] = 0.f;
-            if (cur.f & NF_FIX_Y) y[1] = 0.f;
-            if (cur.f & NF_FIX_Z) y[2] = 0.f;
+            if (f & NF_FIX_X) y[0] = 0.f;
+            if (f & NF_FIX_Y) y[1] = 0.f;
+            if (f & NF_FIX_Z) y[2] = 0.f;
 #pragma unroll
             for (int b = 0; b < 3; ++b) {
                 const int i = n + b * S;
@@ -354,21 +356,23 @@ __global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? 2 : 3) k_fin
                 if (MODE == FM_PLAIN) {
                     a.out32[i] = y[b];
                 } else if (MODE == FM_VCYCLE_DOWN) {
-                    a.out32[i] = cur.r[b] - y[b];                        // r' = r - A (omega D^-1 r)
+                    a.out32[i] = ed.r[b] - y[b];                         // r' = r - A (omega D^-1 r)
                 } else if (MODE == FM_CG_UPDATE_JACOBI) {
                     // previous iteration's update x += alpha p, r -= alpha q (CG_solver.m:32-33),
-                    // then this iteration's Jacobi step (CG_solver.m:18-19) with its dx kept pending
+                    // then this iteration's Jacobi step x += dx, r -= A dx (CG_solver.m:18-19);
+                    // the caller removes the last dx when the solve stops
                     float rinc = y[b];
-                    float rm32 = cur.r[b];
+                    float rm32 = ed.r[b];
+                    float xinc = v;
                     if (!a.first) {
-                        a.x64[i] += (double)(cur.dx[b] + alpha * cur.pp[b]);
-                        rinc = fmaf(alpha, cur.q[b], rinc);
-                        rm32 = fmaf(-alpha, cur.q[b], rm32);
+                        xinc = fmaf(alpha, ed.pp[b], v);
+                        rinc = fmaf(alpha, ed.q[b], rinc);
+                        rm32 = fmaf(-alpha, ed.q[b], rm32);
                     }
-                    const double rn = cur.r64[b] - (double)rinc;
+                    a.x64[i] += (double)xinc;
+                    const double rn = ed.r64[b] - (double)rinc;
                     a.r64[i] = rn;
                     a.r32out[i] = (float)rn;
-                    a.dxp[i] = v;
                     dot.add(rm32 * rm32);
                 } else {
                     a.pout[i] = v;
@@ -419,63 +423,86 @@ __global__ void __launch_bounds__(256) k_up32(Grid gf, Grid gc, const uint8_t* _
                                               const float* __restrict__ rp, const float* __restrict__ xc,
                                               float* __restrict__ xf, int zero_fixed, DotOut dout) {
     __shared__ double sh[32];
-    const int iy = blockIdx.x * blockDim.x + threadIdx.x;
-    const int ix = blockIdx.y * blockDim.y + threadIdx.y;
-    const int iz = blockIdx.z;
+    const int Sf = (int)gf.slots, Sc = (int)gc.slots;
+    const int csx = gc.py, csz = gc.py * gc.px;
+    const int ny1 = gf.ny + 1, nx1 = gf.nx + 1;
+    const int64_t total = (int64_t)ny1 * nx1 * (gf.nz + 1);
     Kahan dot;
-    if (iy <= gf.ny && ix <= gf.nx) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int iy = (int)(t % ny1);
+        const int64_t rest = t / ny1;
+        const int ix = (int)(rest % nx1), iz = (int)(rest / nx1);
         const int fs = (int)gf.slot(iy, ix, iz);
         const uint8_t fl = nflag[fs];
-        if (fl & NF_SOLID) {
-            const int Sf = (int)gf.slots, Sc = (int)gc.slots;
-            const int Iy = iy >> 1, Ix = ix >> 1, Iz = iz >> 1;
-            const int oy = iy & 1, ox = ix & 1, oz = iz & 1;
-            const int c0 = (int)gc.slot(Iy, Ix, Iz);
-            const int csx = gc.py, csz = gc.py * gc.px;
-            const float w = (oy ? 0.5f : 1.f) * (ox ? 0.5f : 1.f) * (oz ? 0.5f : 1.f);
+        if (!(fl & NF_SOLID)) continue;
+        const int Iy = iy >> 1, Ix = ix >> 1, Iz = iz >> 1;
+        const int oy = iy & 1, ox = ix & 1, oz = iz & 1;
+        const int c0 = (int)gc.slot(Iy, Ix, Iz);
+        const float w = (oy ? 0.5f : 1.f) * (ox ? 0.5f : 1.f) * (oz ? 0.5f : 1.f);
 #pragma unroll
-            for (int comp = 0; comp < 3; ++comp) {
-                const float* x = xc + comp * Sc;
-                float v = x[c0];
-                if (oy) v += x[c0 + 1];
-                if (ox) {
-                    v += x[c0 + csx];
-                    if (oy) v += x[c0 + csx + 1];
-                }
-                if (oz) {
-                    v += x[c0 + csz];
-                    if (oy) v += x[c0 + csz + 1];
-                    if (ox) {
-                        v += x[c0 + csz + csx];
-                        if (oy) v += x[c0 + csz + csx + 1];
-                    }
-                }
-                const int i = fs + comp * Sf;
-                const float wd = wdinv[i];
-                const float ri = r[i];
-                float out = (wd * ri + w * v) + wd * rp[i];
-                if (zero_fixed && (fl & (NF_FIX_X << comp))) out = 0.f;
-                xf[i] = out;
-                if (DOT) dot.add(ri * out);
+        for (int comp = 0; comp < 3; ++comp) {
+            const float* x = xc + comp * Sc;
+            float v = x[c0];
+            if (oy) v += x[c0 + 1];
+            if (ox) {
+                v += x[c0 + csx];
+                if (oy) v += x[c0 + csx + 1];
             }
+            if (oz) {
+                v += x[c0 + csz];
+                if (oy) v += x[c0 + csz + 1];
+                if (ox) {
+                    v += x[c0 + csz + csx];
+                    if (oy) v += x[c0 + csz + csx + 1];
+                }
+            }
+            const int i = fs + comp * Sf;
+            const float wd = wdinv[i];
+            const float ri = r[i];
+            float out = (wd * ri + w * v) + wd * rp[i];
+            if (zero_fixed && (fl & (NF_FIX_X << comp))) out = 0.f;
+            xf[i] = out;
+            if (DOT) dot.add(ri * out);
         }
     }
     if (DOT) grid_dot_finish(dot.value(), dout, sh);
 }
 
+static int up32_blocks(const Ctx& c, const Grid& gf) {
+    const int64_t total = (int64_t)(gf.ny + 1) * (gf.nx + 1) * (gf.nz + 1);
+    return (int)std::max<int64_t>(1, std::min<int64_t>((total + 255) / 256, (int64_t)c.num_sms * 8));
+}
+
 void launch_up32(Ctx& c, const Grid& gf, const Grid& gc, const uint8_t* nflag, const float* wdinv, const float* r,
                  const float* rp, const float* xc, float* xf, bool zero_fixed, const DotOut* dot) {
-    dim3 blk(32, 8, 1);
-    dim3 grid((gf.ny + 1 + 31) / 32, (gf.nx + 1 + 7) / 8, gf.nz + 1);
+    const int blocks = up32_blocks(c, gf);
     if (dot) {
-        k_up32<true><<<grid, blk, 0, c.stream>>>(gf, gc, nflag, wdinv, r, rp, xc, xf, zero_fixed, *dot);
+        k_up32<true><<<blocks, 256, 0, c.stream>>>(gf, gc, nflag, wdinv, r, rp, xc, xf, zero_fixed, *dot);
     } else {
-        k_up32<false><<<grid, blk, 0, c.stream>>>(gf, gc, nflag, wdinv, r, rp, xc, xf, zero_fixed, DotOut{});
+        k_up32<false><<<blocks, 256, 0, c.stream>>>(gf, gc, nflag, wdinv, r, rp, xc, xf, zero_fixed, DotOut{});
     }
     GMGS_LAUNCHED(c);
 }
 
-int up32_grid_blocks(const Grid& gf) { return ((gf.ny + 1 + 31) / 32) * ((gf.nx + 1 + 7) / 8) * (gf.nz + 1); }
+int up32_grid_blocks(const Grid& gf) { return 4096; }
+
+// x -= the last, not yet cancelled Jacobi step dx = fl32(fl32(r32 - alpha q) * w)
+__global__ void k_drop_last_dx(int64_t n, double* __restrict__ x, const float* __restrict__ r32,
+                               const float* __restrict__ q, const float* __restrict__ w,
+                               const double* __restrict__ scal, int cur, int first) {
+    const float alpha = first ? 0.f : (float)(scal[cur] / scal[2]);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float rm = first ? r32[i] : fmaf(-alpha, q[i], r32[i]);
+        const float dx = rm * w[i];
+        if (dx != 0.f) x[i] -= (double)dx;
+    }
+}
+void launch_drop_last_dx(Ctx& c, int64_t n, double* x, const float* r32, const float* q, const float* w,
+                         const double* scal, int cur, int first) {
+    const int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)c.num_sms * 16);
+    k_drop_last_dx<<<blocks, 256, 0, c.stream>>>(n, x, r32, q, w, scal, cur, first);
+    GMGS_LAUNCHED(c);
+}
 
 // omega / diag in FP32 (0 where the diagonal is 0)
 __global__ void k_wdinv(int64_t n, const double* __restrict__ d, double omega, float* __restrict__ w) {

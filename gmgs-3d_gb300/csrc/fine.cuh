@@ -33,9 +33,9 @@ struct DotOut {
 enum FineMode {
     FM_PLAIN = 0,             // y = A v
     FM_VCYCLE_DOWN = 1,       // v = w r, out = r - A v               (Vcycle.m:14, JacobiSmoother.m:5-9)
-    FM_CG_UPDATE_JACOBI = 2,  // previous CG update r_m = r - alpha q, x += dx_prev + alpha p,
-                              // r_m.r_m; then v = fl32(w r_m) kept as the pending dx,
-                              // r = r_m - A v                  (CG_solver.m:31-35, 18-19)
+    FM_CG_UPDATE_JACOBI = 2,  // previous CG update r_m = r - alpha q, x += alpha p, r_m.r_m;
+                              // then the Jacobi step v = fl32(w r_m), x += v, r = r_m - A v
+                              //                                  (CG_solver.m:31-35, 18-19)
     FM_CG_DIRECTION = 3       // v = fl32(z + beta p_old), p = v, q = A v, p.q  (CG_solver.m:23-31)
 };
 
@@ -47,7 +47,6 @@ struct FineArgs {
     const float* z32 = nullptr;      // FM_CG_DIRECTION preconditioned residual
     const float* pold = nullptr;     // previous direction (FM_CG_DIRECTION: p_{k-1}; FM_CG_UPDATE_JACOBI: p_k)
     const float* q32 = nullptr;      // FM_CG_UPDATE_JACOBI: q = A p of the previous iteration
-    float* dxp = nullptr;            // FM_CG_UPDATE_JACOBI: pending Jacobi step (read, then overwritten)
     const double* scal = nullptr;    // CG scalars: [0],[1] r.z by parity, [2] p.q
     int cur = 0, first = 0;
     float* out32 = nullptr;          // y / r' / q
@@ -71,5 +70,7 @@ void launch_up32(Ctx& c, const Grid& gf, const Grid& gc, const uint8_t* nflag, c
 void launch_wdinv(Ctx& c, int64_t n, const double* d, double omega, float* w);
 void launch_emask8(Ctx& c, const Grid& g, const uint8_t* emask, uint8_t* e8);
 void launch_to_f32(Ctx& c, int64_t n, const double* a, float* b);
+void launch_drop_last_dx(Ctx& c, int64_t n, double* x, const float* r32, const float* q, const float* w,
+                         const double* scal, int cur, int first);
 
 }  // namespace gmgs

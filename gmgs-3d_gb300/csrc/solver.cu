@@ -64,7 +64,6 @@ void alloc_work(Model& M) {
         zalloc(c, M.cg_q32, n3 * 4);
         zalloc(c, M.cg_z32, n3 * 4);
         zalloc(c, M.cg_r32, n3 * 4);
-        zalloc(c, M.cg_dxp, n3 * 4);
     } else {
         zalloc(c, M.cg_p, n3 * 8);
         zalloc(c, M.cg_dx, n3 * 8);
@@ -221,7 +220,6 @@ static int pcg_mixed(Model& M, const double* b, double* x, int32_t* iters_out, d
     float* r32b = M.cg_r32b.as<float>();
     float* pa = M.cg_pa.as<float>();
     float* pb = M.cg_pb.as<float>();
-    float* dxp = M.cg_dxp.as<float>();
     float* q = M.cg_q32.as<float>();
     const FineLevel f0 = fine_level(l0);
 
@@ -240,14 +238,14 @@ static int pcg_mixed(Model& M, const double* b, double* x, int32_t* iters_out, d
         return GMGS_OK;
     }
     if (!std::isfinite(normB)) throw Error(GMGS_ERR_NONFINITE, "non-finite load vector");
-    // algorithmic bytes per node: r64 rw, r32 read + write, q, p, wdinv, x rw, dxp rw
-    const double jbytes = (double)l0.n_node * 3 * (16 + 8 + 4 + 4 + 4 + 16 + 8) + 2.0 * (double)l0.n_node;
+    // algorithmic bytes per node: r64 rw, r32 read + write, q, p, wdinv, x rw
+    const double jbytes = (double)l0.n_node * 3 * (16 + 8 + 4 + 4 + 4 + 16) + 2.0 * (double)l0.n_node;
     const double pbytes = (double)l0.n_node * 3 * (4 + 4 + 4 + 4) + 2.0 * (double)l0.n_node;
 
     // Fused kernel: the previous iteration's update (x += alpha p, r -= alpha q,
-    // |r|^2 for its convergence test) followed by this iteration's Jacobi step,
-    // whose dx stays pending until the next update, so x is always the
-    // reference's x at the end of the last completed iteration.
+    // |r|^2 for its convergence test) followed by the next iteration's Jacobi
+    // step (x += dx, r -= A dx).  When the solve stops, the last dx (which
+    // belongs to an iteration that does not run) is removed from x again.
     auto update_jacobi = [&](int first, int cur) {
         FineArgs a;
         a.r32 = r32a;
@@ -256,7 +254,6 @@ static int pcg_mixed(Model& M, const double* b, double* x, int32_t* iters_out, d
         a.pold = pa;
         a.wdinv = l0.wdinv32.as<float>();
         a.x64 = x;
-        a.dxp = dxp;
         a.r32out = r32b;
         a.scal = scal;
         a.cur = cur;
@@ -323,6 +320,10 @@ static int pcg_mixed(Model& M, const double* b, double* x, int32_t* iters_out, d
         }
         ++nhist;
     }
+    // the last fused launch already applied the Jacobi step of an iteration
+    // that does not run; its inputs (r32 it read, q, alpha) are still in place
+    launch_drop_last_dx(c, n3, x, r32b, q, l0.wdinv32.as<float>(), scal, its & 1, 0);
+    GMGS_CUDA(cudaStreamSynchronize(c.stream));
     if (status == GMGS_ERR_MAX_ITERATIONS && M.prm.verbose) std::printf("Exceed the maximum iterate numbers\n");
     if (iters_out) *iters_out = its;
     if (relres_out) *relres_out = resnorm;

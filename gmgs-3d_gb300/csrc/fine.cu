@@ -33,8 +33,9 @@ namespace gmgs {
 constexpr int TY = 32, TX = 8;
 constexpr int HY = TY + 2, HX = TX + 2;
 constexpr int NT = TY * TX;
-constexpr int PLANE = HY * HX;          // 340 points
-constexpr int NHALO = PLANE - NT;       // 84 halo points per plane
+constexpr int RP = 40;                  // shared-memory row pitch (>= HY; 8 mod 32 keeps 8x4 warp patches conflict-free)
+constexpr int PLANE = RP * HX;          // floats per component plane (34 x 10 points used)
+constexpr int NHALO = HY * HX - NT;     // 84 halo points per plane
 
 // displacement component a (0 = x, 1 = y, 2 = z) of stencil offset k = (dz+1)*9 + (dx+1)*3 + (dy+1)
 __host__ __device__ constexpr int off_y(int k) { return k % 3 - 1; }
@@ -134,7 +135,7 @@ __device__ __forceinline__ void interior_s(const Coef32& cf, const float* __rest
     float acc[3] = {0.f, 0.f, 0.f};
 #pragma unroll
     for (int k = 14; k < 27; ++k) {
-        const int o = off_y(k) + off_x(k) * HY;
+        const int o = off_y(k) + off_x(k) * RP;
         const float* up = off_z(k) > 0 ? P2 : (off_z(k) < 0 ? P0 : P1);
         const float* dn = off_z(k) > 0 ? P0 : (off_z(k) < 0 ? P2 : P1);
         float d[3];
@@ -163,7 +164,7 @@ __device__ __forceinline__ void elem_rows(const Coef32& cf, const float* __restr
         if (j == CI) continue;
         const int dy = corner_y(j) - A, dx = corner_x(j) - B, dz = corner_z(j) - C;
         const float* pl = dz > 0 ? P2 : (dz < 0 ? P0 : P1);
-        const int q = p + dy + dx * HY;
+        const int q = p + dy + dx * RP;
         const float d0 = pl[q] - c0, d1 = pl[q + PLANE] - c1, d2 = pl[q + 2 * PLANE] - c2;
         float t[3];
 #pragma unroll
@@ -273,26 +274,29 @@ __global__ void __launch_bounds__(NT, 3) k_fine(FineLevel L, const __grid_consta
     const int y0 = blockIdx.x * TY, x0 = blockIdx.y * TX;
     const int zb = blockIdx.z * zc;
     const int ze = min(zb + zc, g.nz + 1);        // node planes [zb, ze)
-    const int tx = threadIdx.x, ty = threadIdx.y;
-    const int tid = tx + ty * TY;
+    // warps cover 8 (y) x 4 (x) node patches, so a face of the domain
+    // crosses few warps and the boundary path rarely diverges
+    const int tid = threadIdx.x + threadIdx.y * TY;
+    const int wrp = tid >> 5, lane = tid & 31;
+    const int ly = (wrp & 3) * 8 + (lane & 7), lx = (wrp >> 2) * 4 + (lane >> 3);
 
     float beta = 0.f, alpha = 0.f;
     if (MODE == FM_CG_DIRECTION && !a.first) beta = (float)(a.scal[a.cur] / a.scal[a.cur ^ 1]);
     if (MODE == FM_CG_UPDATE_JACOBI && !a.first) alpha = (float)(a.scal[a.cur] / a.scal[2]);
 
     // this thread's centre point and (for tid < NHALO) one halo point of every plane
-    const int cy = y0 + tx, cx = x0 + ty;
-    const int pc = (tx + 1) + (ty + 1) * HY;
+    const int cy = y0 + ly, cx = x0 + lx;
+    const int pc = (ly + 1) + (lx + 1) * RP;
     const bool ccol = cy <= g.ny + 1 && cx <= g.nx + 1;
     const int cbase = (cx + 1) * g.py + (cy + 1) + sz;          // slot(cy, cx, iz) = cbase + iz * sz
     int ph = 0, hbase = 0;
     bool hcol = false;
     if (tid < NHALO) {
-        int ly, lx;
-        if (tid < 2 * HX) { ly = (tid & 1) ? HY - 1 : 0; lx = tid >> 1; }
-        else { const int k = tid - 2 * HX; lx = (k & 1) ? HX - 1 : 0; ly = 1 + (k >> 1); }
-        ph = ly + lx * HY;
-        const int hy = y0 - 1 + ly, hx = x0 - 1 + lx;
+        int hy_, hx_;
+        if (tid < 2 * HX) { hy_ = (tid & 1) ? HY - 1 : 0; hx_ = tid >> 1; }
+        else { const int k = tid - 2 * HX; hx_ = (k & 1) ? HX - 1 : 0; hy_ = 1 + (k >> 1); }
+        ph = hy_ + hx_ * RP;
+        const int hy = y0 - 1 + hy_, hx = x0 - 1 + hx_;
         hcol = hy >= -1 && hx >= -1 && hy <= g.ny + 1 && hx <= g.nx + 1;
         hbase = (hx + 1) * g.py + (hy + 1) + sz;
     }

@@ -80,7 +80,7 @@ int64_t model_bytes(const gmgs::Model& M) {
     int64_t b = 0;
     for (const auto& lv : M.levels)
         for (const gmgs::DevBuf* d : {&lv.emask, &lv.nflag, &lv.etype, &lv.escale64, &lv.escale32, &lv.Ks64, &lv.Ks32,
-                                      &lv.kslot, &lv.diag64, &lv.diag32, &lv.wdinv32, &lv.emask8, &lv.node_slot, &lv.elem_slot, &lv.node_count,
+                                      &lv.kslot, &lv.diag64, &lv.diag32, &lv.wdinv32, &lv.emask8, &lv.perel_nodes, &lv.node_slot, &lv.elem_slot, &lv.node_count,
                                       &lv.vr, &lv.vrp, &lv.vdx, &lv.vx, &lv.vy})
             b += (int64_t)d->bytes;
     for (const gmgs::DevBuf* d : {&M.ke0_dev, &M.rho, &M.F, &M.U, &M.free_idx, &M.kinv, &M.cvec_in, &M.cvec_out,

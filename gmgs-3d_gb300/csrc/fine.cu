@@ -339,7 +339,7 @@ __global__ void __launch_bounds__(NT, 3) k_fine(FineLevel L, const __grid_consta
         const float* P0 = ring[(iz + 2) % 3];
         const float* P1 = ring[iz % 3];
         const float* P2 = ring[(iz + 1) % 3];
-        if (own && (f & NF_SOLID)) {
+        if (own && (f & NF_SOLID) && !(f & NF_PEREL)) {
             const int n = cbase + iz * sz;
             EpiData ed;
             epi_fetch<MODE>(a, S, n, ed);       // in flight during the stencil arithmetic
@@ -505,6 +505,65 @@ void launch_drop_last_dx(Ctx& c, int64_t n, double* x, const float* r32, const f
                          const double* scal, int cur, int first) {
     const int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)c.num_sms * 16);
     k_drop_last_dx<<<blocks, 256, 0, c.stream>>>(n, x, r32, q, w, scal, cur, first);
+    GMGS_LAUNCHED(c);
+}
+
+// ---------------------------------------------------------------------------
+// V-cycle down-sweep at nodes that touch elements with their own Galerkin
+// matrix: one warp per node; lane 3e + a computes row (corner, a) of element
+// e (24 coefficients, one contiguous row) against the element's Jacobi step
+// w r, and a shuffle reduction over e sums the node's three rows.
+// out = r - A (w r) with fixed rows of A zeroed (AtX.m:57).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_perel_vdown(FineLevel L, const __grid_constant__ Coef32 cf,
+                                                     const int32_t* __restrict__ nodes, int count,
+                                                     const float* __restrict__ r, const float* __restrict__ w,
+                                                     float* __restrict__ out) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= count) return;
+    const Grid& g = L.g;
+    const int S = (int)g.slots, sx = g.py, sz = g.py * g.px;
+    const int n = nodes[warp];
+    const uint32_t f = L.nflag[n];
+    float part = 0.f;
+    if (lane < 24) {
+        const int e = lane / 3, a = lane - 3 * e;
+        const int A = e & 1, B = (e >> 1) & 1, C = e >> 2;
+        const int es = n - A - B * sx - C * sz;
+        if (L.emask[es]) {
+            const int ci = corner_of(A, B, C);
+            const int t = L.etype ? L.etype[es] : 0;
+            const float* Krow = t > 0 ? L.Ks + (int64_t)(t - 1) * KE + (3 * ci + a) * 24 : nullptr;
+            const float s = t > 0 ? 1.f : L.kscale;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int nj = es + corner_y(j) + corner_x(j) * sx + corner_z(j) * sz;
+#pragma unroll
+                for (int b = 0; b < 3; ++b) {
+                    const int i = nj + b * S;
+                    const float dx = r[i] * w[i];
+                    const float k = t > 0 ? Krow[3 * j + b] : s * cf.K[(3 * ci + a) * 24 + 3 * j + b];
+                    part = fmaf(k, dx, part);
+                }
+            }
+        }
+    }
+    // lanes a, a+3, ..., a+21 hold the 8 element rows of component a
+    float sum = part;
+    for (int k = 1; k < 8; ++k) sum += __shfl_sync(0xffffffffu, part, (lane + 3 * k) & 31);
+    if (lane < 3) {
+        const int i = n + lane * S;
+        const float y = (f & (NF_FIX_X << lane)) ? 0.f : sum;
+        out[i] = r[i] - y;
+    }
+}
+
+void launch_perel_vdown(Ctx& c, const FineLevel& L, const Coef32& cf, const int32_t* nodes, int count, const float* r,
+                        const float* w, float* out) {
+    if (count <= 0) return;
+    const int blocks = (int)(((int64_t)count * 32 + 255) / 256);
+    k_perel_vdown<<<blocks, 256, 0, c.stream>>>(L, cf, nodes, count, r, w, out);
     GMGS_LAUNCHED(c);
 }
 

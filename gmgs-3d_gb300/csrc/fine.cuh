@@ -57,6 +57,7 @@ struct FineArgs {
 };
 
 constexpr uint8_t NF_INTERIOR = 16;
+constexpr uint8_t NF_PEREL = 32;     // node touches an element with its own stored matrix
 
 void make_stencil(const double* ke_rows, Coef32& cf);
 int fine_grid_blocks(const Grid& g);
@@ -68,6 +69,8 @@ void launch_fine(Ctx& c, const FineLevel& L, const Coef32& cf, const FineArgs& a
 void launch_up32(Ctx& c, const Grid& gf, const Grid& gc, const uint8_t* nflag, const float* wdinv, const float* r,
                  const float* rp, const float* xc, float* xf, bool zero_fixed, const DotOut* dot);
 void launch_wdinv(Ctx& c, int64_t n, const double* d, double omega, float* w);
+void launch_perel_vdown(Ctx& c, const FineLevel& L, const Coef32& cf, const int32_t* nodes, int count, const float* r,
+                        const float* w, float* out);
 void launch_emask8(Ctx& c, const Grid& g, const uint8_t* emask, uint8_t* e8);
 void launch_to_f32(Ctx& c, int64_t n, const double* a, float* b);
 void launch_drop_last_dx(Ctx& c, int64_t n, double* x, const float* r32, const float* q, const float* w,

@@ -140,6 +140,8 @@ struct Level {
     DevBuf vr, vrp, vdx, vx, vy;
     DevBuf wdinv32;           // mixed path: omega / diag in FP32
     DevBuf emask8;            // mixed path: per-node mask of the 8 surrounding solid elements
+    DevBuf perel_nodes;       // slots of nodes touching an element with its own stored matrix
+    int64_t n_perel = 0;
 };
 
 // Per-launch CUDA-event timing of selected kernels (diagnostics; off by default).

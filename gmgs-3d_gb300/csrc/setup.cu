@@ -332,20 +332,24 @@ __global__ void k_node_flags(Grid g, const uint8_t* __restrict__ emask, uint8_t*
     }
 }
 
-// nodes whose 8 elements all carry the level's uniform matrix kscale * Ke0
+// NF_INTERIOR: the node's 8 elements all carry the level's uniform matrix
+// kscale * Ke0; NF_PEREL: one of them has its own stored matrix
 __global__ void k_interior_flags(Grid g, const uint8_t* __restrict__ emask, const int32_t* __restrict__ etype,
-                                 uint8_t* __restrict__ nflag) {
+                                 uint8_t* __restrict__ nflag, int32_t* __restrict__ perel) {
     GRID_STRIDE(s, g.slots) {
-        uint8_t f = nflag[s] & (uint8_t)~NF_INTERIOR;
+        uint8_t f = nflag[s] & (uint8_t) ~(NF_INTERIOR | NF_PEREL);
         if (f & NF_SOLID) {
-            bool all = true;
+            bool all = true, pe = false;
             for (int e = 0; e < 8; ++e) {
                 const int64_t es = s - (e & 1) - ((e >> 1) & 1) * g.sx() - (e >> 2) * g.sz();
                 all = all && emask[es] && (!etype || etype[es] == 0);
+                pe = pe || (etype && emask[es] && etype[es] > 0);
             }
             if (all) f |= NF_INTERIOR;
+            if (pe) f |= NF_PEREL;
         }
         nflag[s] = f;
+        if (perel) perel[s] = (f & NF_PEREL) ? 1 : 0;
     }
 }
 
@@ -458,8 +462,10 @@ __global__ void k_diag(Grid g, const uint8_t* __restrict__ emask, const uint8_t*
 // ---------------------------------------------------------------------------
 // boundary conditions
 // ---------------------------------------------------------------------------
+constexpr uint8_t NF_KEEP = NF_SOLID | NF_INTERIOR | NF_PEREL;   // flags that do not depend on the BCs
+
 __global__ void k_clear_fixed(int64_t n, uint8_t* f) {
-    GRID_STRIDE(i, n) f[i] &= (NF_SOLID | NF_INTERIOR);
+    GRID_STRIDE(i, n) f[i] &= NF_KEEP;
 }
 __global__ void k_set_fixed(int64_t n, const int32_t* __restrict__ ids, const int32_t* __restrict__ node_slot,
                             uint8_t* __restrict__ f) {
@@ -477,7 +483,7 @@ __global__ void k_set_loads(int64_t n, const int32_t* __restrict__ ids, const do
 // coarse fixed DOFs: restricted indicator != 0 (SetupSolver.m:247-254)
 __global__ void k_fixed_from_indicator(int64_t S, const double* __restrict__ ind, uint8_t* __restrict__ f) {
     GRID_STRIDE(s, S) {
-        uint8_t v = f[s] & (NF_SOLID | NF_INTERIOR);
+        uint8_t v = f[s] & NF_KEEP;
         if (v & NF_SOLID) {
             if (ind[s] != 0.0) v |= NF_FIX_X;
             if (ind[s + S] != 0.0) v |= NF_FIX_Y;
@@ -695,11 +701,23 @@ void build_operators(Model& M) {
     for (int l = 0; l < L; ++l) {
         Level& lv = M.levels[l];
         const bool uniform_ok = !(l == 0 && lv.escale64.p);
+        lv.n_perel = 0;
         if (uniform_ok) {
+            DevBuf cnt = dalloc(lv.g.slots * sizeof(int32_t));
             k_interior_flags<<<blocks_for(c, lv.g.slots), 256, 0, c.stream>>>(lv.g, lv.emask.as<uint8_t>(),
                                                                                lv.etype.as<int32_t>(),
-                                                                               lv.nflag.as<uint8_t>());
+                                                                               lv.nflag.as<uint8_t>(),
+                                                                               cnt.as<int32_t>());
             GMGS_LAUNCHED(c);
+            if (lv.etype.p) {
+                lv.n_perel = exclusive_scan(c, cnt.as<int32_t>(), lv.g.slots);
+                lv.perel_nodes = dalloc(std::max<int64_t>(1, lv.n_perel) * sizeof(int32_t));
+                k_compact<<<blocks_for(c, lv.g.slots), 256, 0, c.stream>>>(lv.g.slots, lv.nflag.as<uint8_t>(),
+                                                                            NF_PEREL, cnt.as<int32_t>(),
+                                                                            lv.perel_nodes.as<int32_t>());
+                GMGS_LAUNCHED(c);
+            }
+            GMGS_CUDA(cudaStreamSynchronize(c.stream));
         }
     }
     M.ke0_dev = dalloc(KE * sizeof(double));

@@ -182,7 +182,11 @@ static void vcycle32(Model& M, const float* r32, float* z, bool with_dot, int do
             c.mark(PK_VDOWN0, false);
         }
         if (l == 1) c.mark(PK_COARSE, false);
-        launch_fine<FM_VCYCLE_DOWN>(c, fine_level(lv), M.coef, a);
+        const FineLevel fl = fine_level(lv);
+        if (lv.n_perel < lv.n_node) launch_fine<FM_VCYCLE_DOWN>(c, fl, M.coef, a);
+        if (lv.n_perel > 0)
+            launch_perel_vdown(c, fl, M.coef, lv.perel_nodes.as<int32_t>(), (int)lv.n_perel, a.r32, a.wdinv,
+                               a.out32);
         if (l == 0) {
             c.mark(PK_FINE_MATVEC, true, bytes);
             c.mark(PK_VDOWN0, true, bytes);

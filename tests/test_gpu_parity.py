@@ -24,6 +24,8 @@ CASES = {
     "cube12_L3": (lambda: np.ones((12, 12, 12), np.int32), 3, 0.4),
     "block42_L4": (lambda: synthetic.make("block42_fp64")[0], 4, 0.4),
     "ragged_L3": (lambda: synthetic.sphere_voids(21, 13, 18, 6, 7), 3, 0.4),
+    # five levels: level 4 stores one Galerkin matrix per element and is smoothed
+    "block42_L5": (lambda: synthetic.make("block42_fp64")[0], 5, 0.4),
 }
 
 
@@ -92,7 +94,7 @@ def test_stress(solved_pair):
     assert rel(vox, vox_ref) < 1e-5   # FP32 output
 
 
-@pytest.mark.parametrize("name", ["block42_L4", "ragged_L3"])
+@pytest.mark.parametrize("name", ["block42_L4", "ragged_L3", "block42_L5"])
 def test_mixed_precision_error(name):
     o, s = _pair(name, precision="mixed")
     u_ref = o.get_deformation()

@@ -755,8 +755,30 @@ class Oracle:
         per_voxel = (ue @ Mg.T).reshape(-1, 8, 6).mean(axis=1)
         return out, per_voxel
 
+    # ---------------- direct solve (test helper for gradient checks)
+    def direct_solve(self, b=None):
+        """Exact solution of the finest-level system on its free DOFs (sparse LU).
+
+        The reference's PCG targets tol 1e-3 and can stagnate far above
+        machine precision, so finite-difference checks use this instead.
+        """
+        import scipy.sparse as sp
+        import scipy.sparse.linalg as spl
+        if not self._setup_done:
+            self.setup()
+        lv = self.levels[0]
+        b = self.F if b is None else np.asarray(b, float)
+        mats = self.element_matrices(0)
+        rows = np.repeat(lv.eDofMat, 24, axis=1).ravel()
+        cols = np.tile(lv.eDofMat, (1, 24)).ravel()
+        K = sp.csr_matrix((mats.reshape(len(mats), -1).ravel(), (rows, cols)), shape=(lv.numDOFs,) * 2)
+        f = lv.freeDOFs
+        x = np.zeros(lv.numDOFs)
+        x[f] = spl.spsolve(K[f][:, f].tocsc(), b[f])
+        return x
+
     # ---------------- extension: adjoint
-    def gradient(self, u=None, ell=None):
+    def gradient(self, u=None, ell=None, lam=None):
         """dJ/drho_e for J = f^T u (ell None) or J = ell^T u; needs set_density.
 
         dJ/drho_e = -penal * rho_e^(penal-1) * lam_e^T Ke0 u_e with K lam = ell
@@ -766,11 +788,8 @@ class Oracle:
             raise GMGSError("gradient needs a density field")
         u = self.U if u is None else u
         lv = self.levels[0]
-        if ell is None:
-            lam = u
-        else:
-            ell = np.asarray(ell, float)
-            lam = self.cg(ell)
+        if lam is None:
+            lam = u if ell is None else self.cg(np.asarray(ell, float))
         ue = u[lv.eDofMat]
         le = lam[lv.eDofMat]
         energy = np.einsum("ei,ij,ej->e", le, self.Ke0, ue)

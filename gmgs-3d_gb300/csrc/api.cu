@@ -190,7 +190,7 @@ int gmgs_create(const int32_t* occ, int32_t ny, int32_t nx, int32_t nz, const do
         if (L > 16) fail(GMGS_ERR_RESOLUTION, "too many levels");
         const int64_t pny = ((int64_t)ny + f - 1) / f * f, pnx = ((int64_t)nx + f - 1) / f * f,
                       pnz = ((int64_t)nz + f - 1) / f * f;
-        const int64_t slots = (pny + 10) * (pnx + 3) * (pnz + 3);
+        const int64_t slots = (pny + 17) * (pnx + 3) * (pnz + 3);
         if (slots > (int64_t)INT32_MAX) fail(GMGS_ERR_INVALID_ARGUMENT, "grid too large for 32-bit slot indices");
 
         const auto t0 = Clock::now();

@@ -57,6 +57,170 @@ struct FineArgs {
 };
 
 constexpr uint8_t NF_INTERIOR = 16;
+
+// displacement component a (0 = x, 1 = y, 2 = z) of stencil offset k = (dz+1)*9 + (dx+1)*3 + (dy+1)
+__host__ __device__ constexpr int off_y(int k) { return k % 3 - 1; }
+__host__ __device__ constexpr int off_x(int k) { return (k / 3) % 3 - 1; }
+__host__ __device__ constexpr int off_z(int k) { return k / 9 - 1; }
+__host__ __device__ constexpr int off_comp(int k, int a) { return a == 0 ? off_x(k) : (a == 1 ? off_y(k) : off_z(k)); }
+// structural non-zeros of the assembled interior block S(d)[a][b]
+__host__ __device__ constexpr bool s_nonzero(int k, int a, int b) {
+    return a == b || (off_comp(k, a) != 0 && off_comp(k, b) != 0);
+}
+
+// ---------------------------------------------------------------------------
+// reductions
+// ---------------------------------------------------------------------------
+struct Kahan {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float v) {
+        const float y = v - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
+__device__ __forceinline__ double block_sum_d(double v, double* sh) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int tid = threadIdx.x + threadIdx.y * blockDim.x;
+    const int w = tid >> 5, l = tid & 31;
+    if (l == 0) sh[w] = v;
+    __syncthreads();
+    v = 0;
+    if (w == 0) {
+        v = l < (int)((blockDim.x * blockDim.y) >> 5) ? sh[l] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    }
+    __syncthreads();
+    return v;   // valid in thread 0
+}
+
+// deterministic grid reduction: partial per block, the last block sums them in order
+__device__ inline void grid_dot_finish(double v, const DotOut& d, double* sh) {
+    __shared__ bool last;
+    v = block_sum_d(v, sh);
+    const int nthr = blockDim.x * blockDim.y;
+    const int tid = threadIdx.x + threadIdx.y * blockDim.x;
+    const unsigned nb = gridDim.x * gridDim.y * gridDim.z;
+    const unsigned b = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    if (tid == 0) {
+        d.partials[b] = v;
+        __threadfence();
+        last = atomicAdd(d.ticket, 1u) == nb - 1;
+    }
+    __syncthreads();
+    if (last) {
+        __threadfence();
+        double t = 0;
+        for (unsigned i = tid; i < nb; i += nthr) t += __ldcg(d.partials + i);
+        t = block_sum_d(t, sh);
+        if (tid == 0) {
+            *d.out = t;
+            *d.ticket = 0;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// stencil arithmetic on the shared-memory ring
+// ---------------------------------------------------------------------------
+// interior node, second-difference form; P0, P1, P2 = planes z-1, z, z+1
+template <int RP, int PLANE>
+__device__ __forceinline__ void interior_s(const Coef32& cf, const float* __restrict__ P0, const float* __restrict__ P1,
+                                           const float* __restrict__ P2, int p, float& y0, float& y1, float& y2) {
+    const float c0 = P1[p], c1 = P1[p + PLANE], c2 = P1[p + 2 * PLANE];
+    float acc[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int k = 14; k < 27; ++k) {
+        const int o = off_y(k) + off_x(k) * RP;
+        const float* up = off_z(k) > 0 ? P2 : (off_z(k) < 0 ? P0 : P1);
+        const float* dn = off_z(k) > 0 ? P0 : (off_z(k) < 0 ? P2 : P1);
+        float d[3];
+        d[0] = (up[p + o] - c0) + (dn[p - o] - c0);
+        d[1] = (up[p + o + PLANE] - c1) + (dn[p - o + PLANE] - c1);
+        d[2] = (up[p + o + 2 * PLANE] - c2) + (dn[p - o + 2 * PLANE] - c2);
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b)
+                if (s_nonzero(k, a, b)) acc[a] = fmaf(cf.S[k * 9 + 3 * a + b], d[b], acc[a]);
+    }
+    y0 = acc[0]; y1 = acc[1]; y2 = acc[2];
+}
+
+// rows of one element (node at corner CI of the element with origin offset
+// (A, B, C)), first-difference form, coefficients K (row = output DOF) * s
+template <int RP, int PLANE, int A, int B, int C, bool PARAM>
+__device__ __forceinline__ void elem_rows(const Coef32& cf, const float* __restrict__ Kg, float s,
+                                          const float* __restrict__ P0, const float* __restrict__ P1,
+                                          const float* __restrict__ P2, int p, float c0, float c1, float c2,
+                                          float& y0, float& y1, float& y2) {
+    constexpr int CI = corner_of(A, B, C);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        if (j == CI) continue;
+        const int dy = corner_y(j) - A, dx = corner_x(j) - B, dz = corner_z(j) - C;
+        const float* pl = dz > 0 ? P2 : (dz < 0 ? P0 : P1);
+        const int q = p + dy + dx * RP;
+        const float d0 = pl[q] - c0, d1 = pl[q + PLANE] - c1, d2 = pl[q + 2 * PLANE] - c2;
+        float t[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const int r = (3 * CI + a) * 24 + 3 * j;
+            if (PARAM) {
+                t[a] = fmaf(cf.K[r + 2], d2, fmaf(cf.K[r + 1], d1, cf.K[r] * d0));
+            } else {
+                t[a] = fmaf(Kg[r + 2], d2, fmaf(Kg[r + 1], d1, Kg[r] * d0));
+            }
+        }
+        y0 = fmaf(s, t[0], y0);
+        y1 = fmaf(s, t[1], y1);
+        y2 = fmaf(s, t[2], y2);
+    }
+}
+
+template <int RP, int PLANE, int E>
+__device__ __forceinline__ void boundary_elem(const FineLevel& L, const Coef32& cf, uint32_t e8, int n,
+                                              const float* __restrict__ P0, const float* __restrict__ P1,
+                                              const float* __restrict__ P2, int p, float c0, float c1, float c2,
+                                              float& y0, float& y1, float& y2) {
+    constexpr int A = E & 1, B = (E >> 1) & 1, C = E >> 2;
+    if (!((e8 >> E) & 1u)) return;
+    const int es = n - A - B * L.g.py - C * L.g.py * L.g.px;
+    float s = L.kscale;
+    if (L.etype) {
+        const int t = L.etype[es];
+        if (t > 0) {
+            elem_rows<RP, PLANE, A, B, C, false>(cf, L.Ks + (int64_t)(t - 1) * KE, 1.f, P0, P1, P2, p, c0, c1, c2, y0,
+                                                 y1, y2);
+            return;
+        }
+    }
+    if (L.escale) s *= L.escale[es];
+    elem_rows<RP, PLANE, A, B, C, true>(cf, nullptr, s, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);
+}
+
+template <int RP, int PLANE>
+__device__ __forceinline__ void boundary_s(const FineLevel& L, const Coef32& cf, uint32_t e8, int n,
+                                           const float* __restrict__ P0, const float* __restrict__ P1,
+                                           const float* __restrict__ P2, int p, float& y0, float& y1, float& y2) {
+    const float c0 = P1[p], c1 = P1[p + PLANE], c2 = P1[p + 2 * PLANE];
+    y0 = y1 = y2 = 0.f;
+    boundary_elem<RP, PLANE, 0>(L, cf, e8, n, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);
+    boundary_elem<RP, PLANE, 1>(L, cf, e8, n, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);
+    boundary_elem<RP, PLANE, 2>(L, cf, e8, n, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);
+    boundary_elem<RP, PLANE, 3>(L, cf, e8, n, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);
+    boundary_elem<RP, PLANE, 4>(L, cf, e8, n, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);
+    boundary_elem<RP, PLANE, 5>(L, cf, e8, n, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);
+    boundary_elem<RP, PLANE, 6>(L, cf, e8, n, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);
+    boundary_elem<RP, PLANE, 7>(L, cf, e8, n, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);
+}
+
+
 constexpr uint8_t NF_PEREL = 32;     // node touches an element with its own stored matrix
 
 void make_stencil(const double* ke_rows, Coef32& cf);
@@ -65,6 +229,13 @@ int up32_grid_blocks(const Grid& gf);
 
 template <int MODE>
 void launch_fine(Ctx& c, const FineLevel& L, const Coef32& cf, const FineArgs& a);
+
+// four y-nodes per thread (fine4.cu); needs 16-byte aligned rows and a level
+// without per-element matrices
+bool fine4_supported(const Grid& g);
+int fine4_grid_blocks(const Grid& g);
+template <int MODE>
+void launch_fine4(Ctx& c, const FineLevel& L, const Coef32& cf, const FineArgs& a);
 
 void launch_up32(Ctx& c, const Grid& gf, const Grid& gc, const uint8_t* nflag, const float* wdinv, const float* r,
                  const float* rp, const float* xc, float* xf, bool zero_fixed, const DotOut* dot);

@@ -2,9 +2,11 @@
 //
 // Layout in HBM.  Level l has ny x nx x nz (padded) elements and
 // (ny+1) x (nx+1) x (nz+1) nodes.  Nodes live in a dense slot grid with a
-// one-node zero halo on every side, y fastest (the reference's column-major
-// (y, x, z) order, src/common/DiscretizeDesignDomain.m:76):
-//     slot(iy, ix, iz) = ((iz + 1) * px + (ix + 1)) * py + (iy + 1)
+// zero halo on every side, y fastest (the reference's column-major (y, x, z)
+// order, src/common/DiscretizeDesignDomain.m:76):
+//     slot(iy, ix, iz) = ((iz + 1) * px + (ix + 1)) * py + (iy + YOFF)
+// The y halo is YOFF = 4 wide so that node rows start on 16-byte boundaries
+// (groups of 4 y-nodes load as one float4); x and z halos are one node.
 // An element (ey, ex, ez) shares the slot of its lowest-index node, so the 8
 // elements around node n are the slots n - {0,1} * {1, py, py*px}.
 // Vectors are stored as three component planes of `slots` entries (SoA).
@@ -55,6 +57,7 @@ struct Error : std::runtime_error {
 // grid geometry
 // ---------------------------------------------------------------------------
 struct Grid {
+    static constexpr int YOFF = 4;
     int ny = 0, nx = 0, nz = 0;   // elements (padded)
     int py = 0, px = 0, pz = 0;   // slot pitches, halo included
     int64_t slots = 0;
@@ -62,14 +65,21 @@ struct Grid {
     static Grid make(int ny, int nx, int nz) {
         Grid g;
         g.ny = ny; g.nx = nx; g.nz = nz;
-        g.py = ((ny + 3) + 7) / 8 * 8;     // rows start on 32/64-byte boundaries
+        g.py = ((ny + 1 + 2 * YOFF) + 7) / 8 * 8;     // rows start on 32-byte boundaries
         g.px = nx + 3;
         g.pz = nz + 3;
         g.slots = (int64_t)g.py * g.px * g.pz;
         return g;
     }
     __host__ __device__ __forceinline__ int64_t slot(int iy, int ix, int iz) const {
-        return ((int64_t)(iz + 1) * px + (ix + 1)) * py + (iy + 1);
+        return ((int64_t)(iz + 1) * px + (ix + 1)) * py + (iy + YOFF);
+    }
+    // inverse of slot(); halo slots give indices outside [0, n]
+    __host__ __device__ __forceinline__ void coords(int64_t s, int& iy, int& ix, int& iz) const {
+        iy = (int)(s % py) - YOFF;
+        const int64_t r = s / py;
+        ix = (int)(r % px) - 1;
+        iz = (int)(r / px) - 1;
     }
     __host__ __device__ __forceinline__ int64_t sx() const { return py; }
     __host__ __device__ __forceinline__ int64_t sz() const { return (int64_t)py * px; }

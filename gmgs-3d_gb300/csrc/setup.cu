@@ -263,10 +263,7 @@ static int blocks_for(const Ctx& c, int64_t n) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (n); i += (int64_t)gridDim.x * blockDim.x)
 
 __device__ __forceinline__ void slot_coords(const Grid& g, int64_t s, int& iy, int& ix, int& iz) {
-    iy = (int)(s % g.py) - 1;
-    const int64_t r = s / g.py;
-    ix = (int)(r % g.px) - 1;
-    iz = (int)(r / g.px) - 1;
+    g.coords(s, iy, ix, iz);
 }
 
 // ---------------------------------------------------------------------------

@@ -73,7 +73,8 @@ void alloc_work(Model& M) {
     }
     zalloc(c, M.scal, SC_N * sizeof(double));
     M.dot_blocks = M.ctx.num_sms * 4;
-    const int maxb = std::max({M.dot_blocks, fine_grid_blocks(M.levels[0].g), up32_grid_blocks(M.levels[0].g)});
+    const int maxb = std::max({M.dot_blocks, fine_grid_blocks(M.levels[0].g), fine4_grid_blocks(M.levels[0].g),
+                               up32_grid_blocks(M.levels[0].g)});
     zalloc(c, M.dot_partials, (size_t)maxb * sizeof(double));
     zalloc(c, M.dot_ticket, sizeof(unsigned int));
     if (!M.scal_host) GMGS_CUDA(cudaMallocHost(&M.scal_host, SC_N * sizeof(double)));
@@ -156,6 +157,15 @@ static FineLevel fine_level(const Level& lv) {
     return f;
 }
 
+// finest-level launches use the four-nodes-per-thread kernels when the level
+// has uniform element matrices
+template <int MODE>
+static void launch_l0(Model& M, const FineLevel& f, const FineArgs& a) {
+    const Level& l0 = M.levels[0];
+    if (fine4_supported(l0.g) && l0.n_perel == 0) launch_fine4<MODE>(M.ctx, f, M.coef, a);
+    else launch_fine<MODE>(M.ctx, f, M.coef, a);
+}
+
 static DotOut dot_out(Model& M, int slot) {
     DotOut d;
     d.partials = M.dot_partials.as<double>();
@@ -183,7 +193,8 @@ static void vcycle32(Model& M, const float* r32, float* z, bool with_dot, int do
         }
         if (l == 1) c.mark(PK_COARSE, false);
         const FineLevel fl = fine_level(lv);
-        if (lv.n_perel < lv.n_node) launch_fine<FM_VCYCLE_DOWN>(c, fl, M.coef, a);
+        if (l == 0) launch_l0<FM_VCYCLE_DOWN>(M, fl, a);
+        else if (lv.n_perel < lv.n_node) launch_fine<FM_VCYCLE_DOWN>(c, fl, M.coef, a);
         if (lv.n_perel > 0)
             launch_perel_vdown(c, fl, M.coef, lv.perel_nodes.as<int32_t>(), (int)lv.n_perel, a.r32, a.wdinv,
                                a.out32);
@@ -265,7 +276,7 @@ static int pcg_mixed(Model& M, const double* b, double* x, int32_t* iters_out, d
         a.dot = dot_out(M, SC_RR);
         c.mark(PK_FINE_MATVEC, false);
         c.mark(PK_UPDATE_JACOBI, false);
-        launch_fine<FM_CG_UPDATE_JACOBI>(c, f0, M.coef, a);
+        launch_l0<FM_CG_UPDATE_JACOBI>(M, f0, a);
         c.mark(PK_FINE_MATVEC, true, jbytes);
         c.mark(PK_UPDATE_JACOBI, true, jbytes);
         std::swap(r32a, r32b);
@@ -293,7 +304,7 @@ static int pcg_mixed(Model& M, const double* b, double* x, int32_t* iters_out, d
             a.dot = dot_out(M, SC_PQ);
             c.mark(PK_FINE_MATVEC, false);
             c.mark(PK_DIRECTION, false);
-            launch_fine<FM_CG_DIRECTION>(c, f0, M.coef, a);
+            launch_l0<FM_CG_DIRECTION>(M, f0, a);
             c.mark(PK_FINE_MATVEC, true, pbytes);
             c.mark(PK_DIRECTION, true, pbytes);
             std::swap(pa, pb);

@@ -20,7 +20,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = ROOT / "_build" / "gmgs"
 LIB = PKG / "gmgs" / "libgmgs.so"
-SOURCES = ["api.cu", "setup.cu", "operators.cu", "solver.cu", "post.cu", "fine.cu", "fine4.cu", "noalloc.cu"]
+SOURCES = ["api.cu", "setup.cu", "operators.cu", "solver.cu", "post.cu", "fine.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

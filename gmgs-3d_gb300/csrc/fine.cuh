@@ -230,13 +230,6 @@ int up32_grid_blocks(const Grid& gf);
 template <int MODE>
 void launch_fine(Ctx& c, const FineLevel& L, const Coef32& cf, const FineArgs& a);
 
-// four y-nodes per thread (fine4.cu); needs 16-byte aligned rows and a level
-// without per-element matrices
-bool fine4_supported(const Grid& g);
-int fine4_grid_blocks(const Grid& g);
-template <int MODE>
-void launch_fine4(Ctx& c, const FineLevel& L, const Coef32& cf, const FineArgs& a);
-
 void launch_up32(Ctx& c, const Grid& gf, const Grid& gc, const uint8_t* nflag, const float* wdinv, const float* r,
                  const float* rp, const float* xc, float* xf, bool zero_fixed, const DotOut* dot);
 void launch_wdinv(Ctx& c, int64_t n, const double* d, double omega, float* w);

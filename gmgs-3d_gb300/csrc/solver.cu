@@ -73,8 +73,7 @@ void alloc_work(Model& M) {
     }
     zalloc(c, M.scal, SC_N * sizeof(double));
     M.dot_blocks = M.ctx.num_sms * 4;
-    const int maxb = std::max({M.dot_blocks, fine_grid_blocks(M.levels[0].g), fine4_grid_blocks(M.levels[0].g),
-                               up32_grid_blocks(M.levels[0].g)});
+    const int maxb = std::max({M.dot_blocks, fine_grid_blocks(M.levels[0].g), up32_grid_blocks(M.levels[0].g)});
     zalloc(c, M.dot_partials, (size_t)maxb * sizeof(double));
     zalloc(c, M.dot_ticket, sizeof(unsigned int));
     if (!M.scal_host) GMGS_CUDA(cudaMallocHost(&M.scal_host, SC_N * sizeof(double)));
@@ -157,13 +156,9 @@ static FineLevel fine_level(const Level& lv) {
     return f;
 }
 
-// finest-level launches use the four-nodes-per-thread kernels when the level
-// has uniform element matrices
 template <int MODE>
 static void launch_l0(Model& M, const FineLevel& f, const FineArgs& a) {
-    const Level& l0 = M.levels[0];
-    if (fine4_supported(l0.g) && l0.n_perel == 0) launch_fine4<MODE>(M.ctx, f, M.coef, a);
-    else launch_fine<MODE>(M.ctx, f, M.coef, a);
+    launch_fine<MODE>(M.ctx, f, M.coef, a);
 }
 
 static DotOut dot_out(Model& M, int slot) {

@@ -125,6 +125,13 @@ class Solver:
         self._check(self._lib.gmgs_padded_dims(self._h, d))
         return tuple(d)
 
+    @staticmethod
+    def memory_stats(reset_peak: bool = False):
+        """(bytes held now, high-water mark) over every handle in the process."""
+        cur, peak = C.c_int64(), C.c_int64()
+        L.load().gmgs_memory_stats(C.byref(cur), C.byref(peak), int(reset_peak))
+        return cur.value, peak.value
+
     @property
     def device_bytes(self) -> int:
         v = C.c_int64()
@@ -164,8 +171,17 @@ class Solver:
     def set_bc(self, fixed_nodes, loads):
         fixed = np.ascontiguousarray(np.asarray(fixed_nodes).ravel(), dtype=np.int32)
         ld = np.ascontiguousarray(np.asarray(loads, dtype=np.float64).reshape(-1, 4))
+        self._loads = ld
         self._check(self._lib.gmgs_set_bc(self._h, _iptr(fixed) if fixed.size else None, fixed.size,
                                           _dptr(ld) if ld.size else None, ld.shape[0]))
+
+    def load_vector(self):
+        """F (3*num_nodes, interleaved) as ApplyBoundaryCondition.m:7-10 builds it."""
+        F = np.zeros(3 * self.num_nodes(1))
+        for row in self._loads:               # a later duplicate id wins
+            i = 3 * (int(row[0]) - 1)
+            F[i:i + 3] = row[1:4]
+        return F
 
     def set_density(self, rho, penal: float = 3.0):
         r = np.ascontiguousarray(np.asarray(rho, dtype=np.float64).ravel())
@@ -201,6 +217,14 @@ class Solver:
         vox = np.empty((self.num_elements(1), 6), dtype=np.float32) if per_voxel else None
         self._check(self._lib.gmgs_stress(self._h, _dptr(nodal), _fptr(vox)))
         return (nodal, vox) if per_voxel else nodal
+
+    def stress_dev(self, nodal_ptr: int | None, voxel_ptr: int | None):
+        """Stress into device buffers: nodal (num_nodes x 6 f64) and/or per voxel (num_elements x 6 f32)."""
+        self._check(self._lib.gmgs_stress_dev(self._h, C.c_void_p(nodal_ptr or 0), C.c_void_p(voxel_ptr or 0)))
+
+    def grad_dev(self, ell_ptr: int | None, out_ptr: int):
+        """dJ/drho into a device buffer (num_elements f64); ell_ptr None means compliance."""
+        self._check(self._lib.gmgs_grad_dev(self._h, C.c_void_p(ell_ptr or 0), C.c_void_p(out_ptr)))
 
     def grad(self, ell=None):
         out = np.empty(self.num_elements(1))

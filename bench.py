@@ -39,6 +39,12 @@ CLOCK_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.a
                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
 
+# DRAM bytes (read + write) per solid node of one k_fine<FM_CG_UPDATE_JACOBI>
+# launch, from an ncu capture of the same kernel at half resolution (the
+# traffic grows with the node count); None until measured.
+UJ_TRAFFIC_PER_NODE = None
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -120,6 +126,8 @@ fixed, loads = synthetic.boundary_conditions(vox, L)
 t0 = time.perf_counter()
 o = Oracle(vox, Params(omega=omega, num_levels=L, max_it=iters - 1))
 o.apply_boundary_condition(fixed, loads)
+if w.rho_range is not None:
+    o.set_density(synthetic.density(int(vox.sum()), w.rho_range, w.seed), w.penal)
 o.setup()
 t1 = time.perf_counter()
 with np.errstate(all='ignore'):
@@ -209,6 +217,8 @@ def run_gmgs(a):
     s = Solver(vox, omega=a.omega, num_levels=L, tol=w.tol, precision="mixed")
     s.set_stream(stream.cuda_stream)
     s.set_bc(fixed, loads)
+    if rho is not None:
+        s.set_density(rho, 3.0)
     nn = s.num_nodes(1)
     dofs = 3 * nn
 
@@ -236,7 +246,7 @@ def run_gmgs(a):
     launches = s.launch_count - l0
     its = s.iterations
     relres = s.relres
-    nl, mv_ms, mv_bytes = s.kernel_time(0)
+    nl, mv_ms, mv_bytes = s.kernel_time(3)    # finest CG update + Jacobi: the largest share of the launch list
     phase_names = {1: "vcycle", 2: "cg_iteration", 3: "fine_update_jacobi", 4: "fine_vcycle_down",
                    5: "fine_direction", 6: "fine_prolong_post", 7: "coarse_levels"}
     breakdown = {}
@@ -251,16 +261,58 @@ def run_gmgs(a):
         ms = float(t.item())
 
     out = {}
+    if rank == 0:
+        # stress recovery on the solved state: nodal (f64) + per-voxel (6 f32)
+        s.solve_dev(None)
+        ne = s.num_elements(1)
+        nod = torch.empty((nn, 6), dtype=torch.float64, device="cuda")
+        vox6 = torch.empty((ne, 6), dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        s.stress_dev(nod.data_ptr(), vox6.data_ptr())      # warm-up
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        s.stress_dev(nod.data_ptr(), vox6.data_ptr())
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        st_ms = ev0.elapsed_time(ev1)
+        st_bytes = nn * (24 + 48) + ne * 24
+        out["stress"] = {"ms": st_ms, "algorithmic_bytes": st_bytes, "gbs": st_bytes / (st_ms / 1e3) / 1e9}
+        del nod, vox6
+    if rho is not None and rank == 0:
+        # adjoint: compliance gradient (no extra solve) and the z-displacement of
+        # the first loaded node (one adjoint PCG solve), both on the solved state
+        s.solve_dev(None)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        g = s.grad()
+        t_c = time.perf_counter() - t0
+        ell = np.zeros(dofs)
+        ell[3 * (int(loads[0, 0]) - 1) + 2] = 1.0
+        t0 = time.perf_counter()
+        s.grad(ell)
+        t_t = time.perf_counter() - t0
+        out["adjoint"] = {"compliance_grad_s": t_c, "tip_grad_s_incl_adjoint_solve": t_t,
+                          "adjoint_iterations": s.iterations, "grad_max_abs": float(np.abs(g).max()),
+                          "grad_all_nonpositive": bool(np.all(g <= 0))}
+    mem_now, mem_peak = Solver.memory_stats()
+    out["memory"] = {"held_bytes": mem_now, "peak_bytes": mem_peak}
     if rank == 0 and not a.no_fp64:
         u_mixed = s.solve()
+        sig_mixed = s.stress(per_voxel=False)
         s64 = Solver(vox, omega=a.omega, num_levels=L, tol=w.tol, precision="fp64")
         s64.set_stream(stream.cuda_stream)
         s64.set_bc(fixed, loads)
+        if rho is not None:
+            s64.set_density(rho, 3.0)
         ms64 = timed(s64, 1)
         u64 = s64.solve()
+        sig64 = s64.stress(per_voxel=False)
         out["fp64"] = {"seconds": ms64 / 1e3, "iterations": s64.iterations, "relres": s64.relres,
                        "speedup_mixed_vs_fp64": ms64 / ms,
-                       "displacement_rel_err_mixed_vs_fp64": float(np.linalg.norm(u_mixed - u64) / np.linalg.norm(u64))}
+                       "displacement_rel_err_mixed_vs_fp64": float(np.linalg.norm(u_mixed - u64) / np.linalg.norm(u64)),
+                       "displacement_max_err_mixed_vs_fp64": float(np.abs(u_mixed - u64).max() / np.abs(u64).max()),
+                       "stress_rel_err_mixed_vs_fp64": float(np.linalg.norm(sig_mixed - sig64) / np.linalg.norm(sig64))}
         n64, ms64_mv, b64 = s64.kernel_time(0)
         out["fp64"]["fine_matvec_ms_per_launch"] = ms64_mv / max(n64, 1)
         s64.close()
@@ -268,13 +320,15 @@ def run_gmgs(a):
     e2e = None
     if rank == 0 and not a.no_e2e:
         occ_bytes = vox.size * 4
-        bc_bytes = fixed.size * 4 + loads.size * 8
+        bc_bytes = fixed.size * 4 + loads.size * 8 + (rho.size * 8 if rho is not None else 0)
         times = []
         for i in range(2):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             se = Solver(vox, omega=a.omega, num_levels=L, tol=w.tol, precision="mixed")
             se.set_bc(fixed, loads)
+            if rho is not None:
+                se.set_density(rho, 3.0)
             u = se.solve()
             torch.cuda.synchronize()
             times.append(time.perf_counter() - t0)
@@ -313,8 +367,10 @@ def run_gmgs(a):
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "dof_iterations_per_s": dofs * its / (ms / 1e3),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm if achieved else None, "traffic": None,
-                     "kernel": "finest-level K*x", "launches_timed": nl,
+                     "frac": achieved / hbm if achieved else None,
+                     "traffic": UJ_TRAFFIC_PER_NODE * nn if UJ_TRAFFIC_PER_NODE else None,
+                     "kernel": "k_fine<FM_CG_UPDATE_JACOBI> (finest CG update + Jacobi step + K dx)",
+                     "algorithmic_bytes_per_node": 158, "launches_timed": nl,
                      "ms_per_launch": mv_ms / max(nl, 1), "peak_source": peak_note},
         "gpu_launches": launches,
         "breakdown": breakdown,

@@ -80,12 +80,12 @@ int64_t model_bytes(const gmgs::Model& M) {
     int64_t b = 0;
     for (const auto& lv : M.levels)
         for (const gmgs::DevBuf* d : {&lv.emask, &lv.nflag, &lv.etype, &lv.escale64, &lv.escale32, &lv.Ks64, &lv.Ks32,
-                                      &lv.kslot, &lv.diag64, &lv.diag32, &lv.wdinv32, &lv.emask8, &lv.perel_nodes, &lv.node_slot, &lv.elem_slot, &lv.node_count,
+                                      &lv.kslot, &lv.diag64, &lv.diag32, &lv.wdinv32, &lv.emask8, &lv.perel_nodes, &lv.node_slot, &lv.elem_slot,
                                       &lv.vr, &lv.vrp, &lv.vdx, &lv.vx, &lv.vy})
             b += (int64_t)d->bytes;
     for (const gmgs::DevBuf* d : {&M.ke0_dev, &M.rho, &M.F, &M.U, &M.free_idx, &M.kinv, &M.cvec_in, &M.cvec_out,
                                   &M.cg_x, &M.cg_r, &M.cg_p, &M.cg_dx, &M.cg_q64, &M.cg_y64, &M.cg_z64, &M.cg_q32,
-                                  &M.cg_y32, &M.cg_z32, &M.cg_r32, &M.cg_r32b, &M.cg_pa, &M.cg_pb, &M.cg_dxp, &M.scal, &M.dot_partials, &M.dot_ticket})
+                                  &M.cg_y32, &M.cg_z32, &M.cg_r32, &M.cg_r32b, &M.cg_pa, &M.cg_pb, &M.scal, &M.dot_partials, &M.dot_ticket})
         b += (int64_t)d->bytes;
     return b;
 }
@@ -499,6 +499,13 @@ int gmgs_set_tolerance(gmgs_handle* h, double tol, int32_t max_it) {
 int gmgs_device_bytes(const gmgs_handle* h, int64_t* out) {
     if (!h || !out) return GMGS_ERR_INVALID_ARGUMENT;
     *out = model_bytes(h->M);
+    return GMGS_OK;
+}
+
+int gmgs_memory_stats(int64_t* current_bytes, int64_t* peak_bytes, int32_t reset_peak) {
+    if (current_bytes) *current_bytes = gmgs::g_dev_bytes.load();
+    if (peak_bytes) *peak_bytes = gmgs::g_dev_peak.load();
+    if (reset_peak) gmgs::g_dev_peak.store(gmgs::g_dev_bytes.load());
     return GMGS_OK;
 }
 

@@ -351,10 +351,12 @@ void launch_drop_last_dx(Ctx& c, int64_t n, double* x, const float* r32, const f
 
 // ---------------------------------------------------------------------------
 // V-cycle down-sweep at nodes that touch elements with their own Galerkin
-// matrix: one warp per node; lane 3e + a computes row (corner, a) of element
-// e (24 coefficients, one contiguous row) against the element's Jacobi step
-// w r, and a shuffle reduction over e sums the node's three rows.
-// out = r - A (w r) with fixed rows of A zeroed (AtX.m:57).
+// matrix: one warp per node.  For each of the node's 8 elements the warp
+// reads the node's three rows of the element matrix (72 consecutive floats):
+// lane 8a + j takes row a, columns 3j..3j+2, i.e. the coupling of component a
+// to element node j, and multiplies it with node j's Jacobi step w r.  Each
+// lane keeps one row across the 8 elements; a shuffle reduction over the 8
+// lanes of a row sums it.  out = r - A (w r) with fixed rows zeroed (AtX.m:57).
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_perel_vdown(FineLevel L, const __grid_constant__ Coef32 cf,
                                                      const int32_t* __restrict__ nodes, int count,
@@ -367,35 +369,34 @@ __global__ void __launch_bounds__(256) k_perel_vdown(FineLevel L, const __grid_c
     const int S = (int)g.slots, sx = g.py, sz = g.py * g.px;
     const int n = nodes[warp];
     const uint32_t f = L.nflag[n];
+    const int a = lane >> 3, j = lane & 7;      // lanes 24..31 idle (a == 3)
     float part = 0.f;
-    if (lane < 24) {
-        const int e = lane / 3, a = lane - 3 * e;
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
         const int A = e & 1, B = (e >> 1) & 1, C = e >> 2;
         const int es = n - A - B * sx - C * sz;
-        if (L.emask[es]) {
+        if (!L.emask[es]) continue;                 // uniform across the warp
+        if (a < 3) {
             const int ci = corner_of(A, B, C);
             const int t = L.etype ? L.etype[es] : 0;
-            const float* Krow = t > 0 ? L.Ks + (int64_t)(t - 1) * KE + (3 * ci + a) * 24 : nullptr;
-            const float s = t > 0 ? 1.f : L.kscale;
-#pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                const int nj = es + corner_y(j) + corner_x(j) * sx + corner_z(j) * sz;
-#pragma unroll
-                for (int b = 0; b < 3; ++b) {
-                    const int i = nj + b * S;
-                    const float dx = r[i] * w[i];
-                    const float k = t > 0 ? Krow[3 * j + b] : s * cf.K[(3 * ci + a) * 24 + 3 * j + b];
-                    part = fmaf(k, dx, part);
-                }
+            const int nj = es + corner_y(j) + corner_x(j) * sx + corner_z(j) * sz;
+            const float d0 = r[nj] * w[nj], d1 = r[nj + S] * w[nj + S], d2 = r[nj + 2 * S] * w[nj + 2 * S];
+            const int off = (3 * ci + a) * 24 + 3 * j;
+            if (t > 0) {
+                const float* K = L.Ks + (int64_t)(t - 1) * KE + off;
+                part = fmaf(K[0], d0, fmaf(K[1], d1, fmaf(K[2], d2, part)));
+            } else {
+                const float k = L.kscale;
+                part = fmaf(k * cf.K[off], d0, fmaf(k * cf.K[off + 1], d1, fmaf(k * cf.K[off + 2], d2, part)));
             }
         }
     }
-    // lanes a, a+3, ..., a+21 hold the 8 element rows of component a
-    float sum = part;
-    for (int k = 1; k < 8; ++k) sum += __shfl_sync(0xffffffffu, part, (lane + 3 * k) & 31);
-    if (lane < 3) {
-        const int i = n + lane * S;
-        const float y = (f & (NF_FIX_X << lane)) ? 0.f : sum;
+    part += __shfl_xor_sync(0xffffffffu, part, 1);
+    part += __shfl_xor_sync(0xffffffffu, part, 2);
+    part += __shfl_xor_sync(0xffffffffu, part, 4);
+    if (a < 3 && j == 0) {
+        const int i = n + a * S;
+        const float y = (f & (NF_FIX_X << a)) ? 0.f : part;
         out[i] = r[i] - y;
     }
 }

@@ -15,6 +15,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <atomic>
 #include <cstdint>
 #include <cstdio>
 #include <stdexcept>
@@ -117,6 +118,15 @@ struct LevelView {
 // ---------------------------------------------------------------------------
 // host-side level storage
 // ---------------------------------------------------------------------------
+// Device bytes held by every DevBuf in the process, and the high-water mark.
+inline std::atomic<int64_t> g_dev_bytes{0}, g_dev_peak{0};
+inline void count_alloc(int64_t b) {
+    const int64_t now = g_dev_bytes.fetch_add(b) + b;
+    int64_t pk = g_dev_peak.load();
+    while (now > pk && !g_dev_peak.compare_exchange_weak(pk, now)) {
+    }
+}
+
 struct DevBuf {
     void* p = nullptr;
     size_t bytes = 0;
@@ -129,7 +139,11 @@ struct DevBuf {
         return *this;
     }
     ~DevBuf() { release(); }
-    void release() { if (p) cudaFree(p); p = nullptr; bytes = 0; }
+    void release() {
+        if (p) { cudaFree(p); g_dev_bytes.fetch_sub((int64_t)bytes); }
+        p = nullptr;
+        bytes = 0;
+    }
     template <typename T> T* as() const { return static_cast<T*>(p); }
 };
 
@@ -145,7 +159,6 @@ struct Level {
     DevBuf diag64, diag32;
     DevBuf node_slot;         // compact node id -> slot (int32), reference nodMapBack order
     DevBuf elem_slot;         // compact element id -> slot (int32), eleMapBack order
-    DevBuf node_count;        // finest level: solid elements per node (numNod2ElesVec_)
     // V-cycle work vectors (3 planes each), precision of the V-cycle
     DevBuf vr, vrp, vdx, vx, vy;
     DevBuf wdinv32;           // mixed path: omega / diag in FP32

@@ -103,7 +103,7 @@ static void strain_matrix(const double ele[3], double B[48][24], double detJ[8])
 }
 
 void element_stiffness(double E, double nu, const double ele[3], double Ke[576]) {
-    static double B[48][24];
+    double B[48][24];
     double detJ[8], S[6][6];
     strain_matrix(ele, B, detJ);
     hooke(E, nu, S);
@@ -124,35 +124,15 @@ void element_stiffness(double E, double nu, const double ele[3], double Ke[576])
         }
 }
 
-void stress_matrices(double E, double nu, const double ele[3], double Mn[48 * 24], double Mg[48 * 24]) {
-    static double B[48][24];
-    double detJ[8], S[6][6];
-    strain_matrix(ele, B, detJ);
+void stress_coefficients(double E, double nu, const double ele[3], double c[6]) {
+    double S[6][6];
     hooke(E, nu, S);
-    double DB[48][24];
-    for (int g = 0; g < 8; ++g)
-        for (int a = 0; a < 6; ++a)
-            for (int j = 0; j < 24; ++j) {
-                double v = 0;
-                for (int b = 0; b < 6; ++b) v += S[a][b] * B[6 * g + b][j];
-                DB[6 * g + a][j] = v;
-            }
-    // OTP = inv(kron(N, I6)) = kron(inv(N), I6)   (GetCartesianStress.m:44-73)
-    double N[64], Ni[64];
-    for (int g = 0; g < 8; ++g) {
-        const double s = kGauss * kSign[g][0], t = kGauss * kSign[g][1], p = kGauss * kSign[g][2];
-        for (int k = 0; k < 8; ++k)
-            N[g * 8 + k] = 0.125 * (1 + s * kSign[k][0]) * (1 + t * kSign[k][1]) * (1 + p * kSign[k][2]);
-    }
-    invert(8, N, Ni);
-    for (int k = 0; k < 8; ++k)
-        for (int a = 0; a < 6; ++a)
-            for (int j = 0; j < 24; ++j) {
-                double v = 0;
-                for (int g = 0; g < 8; ++g) v += Ni[k * 8 + g] * DB[6 * g + a][j];
-                Mn[(6 * k + a) * 24 + j] = v;
-                Mg[(6 * k + a) * 24 + j] = DB[6 * k + a][j];
-            }
+    c[0] = S[0][0];        // isotropic D: d11 on the normal diagonal,
+    c[1] = S[0][1];        // d12 off it,
+    c[2] = S[3][3];        // d44 on the engineering shear strains
+    c[3] = 1.0 / ele[0];
+    c[4] = 1.0 / ele[1];
+    c[5] = 1.0 / ele[2];
 }
 
 // ---------------------------------------------------------------------------
@@ -250,6 +230,7 @@ DevBuf dalloc(size_t bytes) {
     if (bytes == 0) bytes = 16;
     GMGS_CUDA(cudaMalloc(&b.p, bytes));
     b.bytes = bytes;
+    count_alloc((int64_t)bytes);
     return b;
 }
 
@@ -386,7 +367,7 @@ __device__ __forceinline__ double tri_w(int pos, int corner2) {
 
 __global__ void __launch_bounds__(192) k_galerkin(Grid gc, Grid gf, const int32_t* __restrict__ kslot,
                                                   const uint8_t* __restrict__ emf, const int32_t* __restrict__ etf,
-                                                  const double* __restrict__ Ksf, const double* __restrict__ ke0,
+                                                  const double* __restrict__ Ksf, const double* __restrict__ G,
                                                   double kscale_f, const double* __restrict__ escale_f,
                                                   double* __restrict__ Ks_out) {
     __shared__ double K[KE], T[KE], W[64];
@@ -399,9 +380,12 @@ __global__ void __launch_bounds__(192) k_galerkin(Grid gc, Grid gf, const int32_
         const int64_t fs = gf.slot(2 * Ey + dy, 2 * Ex + dx, 2 * Ez + dz);
         if (!emf[fs]) continue;       // uniform branch across the block
         const int t = etf ? etf[fs] : 0;
-        const double sc = kscale_f * (escale_f ? escale_f[fs] : 1.0);
-        for (int i = threadIdx.x; i < KE; i += blockDim.x)
-            K[i] = t > 0 ? Ksf[(int64_t)(t - 1) * KE + i] : sc * ke0[i];
+        if (t == 0) {                 // a scaled Ke0 child: sc * (P_j^T Ke0 P_j), precomputed
+            const double sc = kscale_f * (escale_f ? escale_f[fs] : 1.0);
+            for (int k = 0; k < 3; ++k) acc[k] += sc * G[j * KE + threadIdx.x + k * blockDim.x];
+            continue;
+        }
+        for (int i = threadIdx.x; i < KE; i += blockDim.x) K[i] = Ksf[(int64_t)(t - 1) * KE + i];
         if (threadIdx.x < 64) {
             const int q = threadIdx.x >> 3, b = threadIdx.x & 7;   // W[q][b]: corner b at child-local node q
             W[threadIdx.x] = tri_w(dy + corner_y(q), 2 * corner_y(b)) * tri_w(dx + corner_x(q), 2 * corner_x(b)) *
@@ -567,10 +551,6 @@ __global__ void k_symmetrize_lower(int n, double* A) {
 __global__ void k_to_float(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
     GRID_STRIDE(i, n) b[i] = (float)a[i];
 }
-__global__ void k_node_count_compact(int64_t nn, const int32_t* __restrict__ node_slot, const int32_t* __restrict__ cnt,
-                                     double* __restrict__ out) {
-    GRID_STRIDE(i, nn) out[i] = (double)cnt[node_slot[i]];
-}
 
 // ---------------------------------------------------------------------------
 // host orchestration
@@ -628,9 +608,8 @@ void build_levels(Model& M, const int32_t* occ_dev) {
     // node flags, compact node maps, element counts
     for (int l = 0; l < L; ++l) {
         Level& lv = M.levels[l];
-        DevBuf cnt = dalloc(lv.g.slots * sizeof(int32_t));
         k_node_flags<<<blocks_for(c, lv.g.slots), 256, 0, c.stream>>>(lv.g, lv.emask.as<uint8_t>(),
-                                                                       lv.nflag.as<uint8_t>(), cnt.as<int32_t>());
+                                                                       lv.nflag.as<uint8_t>(), nullptr);
         GMGS_LAUNCHED(c);
         DevBuf sc = dalloc(lv.g.slots * sizeof(int32_t));
         k_flag_to_count<<<blocks_for(c, lv.g.slots), 256, 0, c.stream>>>(lv.g.slots, lv.nflag.as<uint8_t>(), NF_SOLID,
@@ -650,12 +629,6 @@ void build_levels(Model& M, const int32_t* occ_dev) {
         k_compact<<<blocks_for(c, lv.g.slots), 256, 0, c.stream>>>(lv.g.slots, lv.emask.as<uint8_t>(), 1,
                                                                     sc.as<int32_t>(), lv.elem_slot.as<int32_t>());
         GMGS_LAUNCHED(c);
-        if (l == 0) {
-            lv.node_count = dalloc(std::max<int64_t>(1, lv.n_node) * sizeof(double));
-            k_node_count_compact<<<blocks_for(c, lv.n_node), 256, 0, c.stream>>>(
-                lv.n_node, lv.node_slot.as<int32_t>(), cnt.as<int32_t>(), lv.node_count.as<double>());
-            GMGS_LAUNCHED(c);
-        }
         GMGS_CUDA(cudaStreamSynchronize(c.stream));
     }
     if (M.levels[0].n_elem == 0) throw Error(GMGS_ERR_NO_SOLID, "the occupancy has no solid voxel");
@@ -720,6 +693,34 @@ void build_operators(Model& M) {
     M.ke0_dev = dalloc(KE * sizeof(double));
     GMGS_CUDA(cudaMemcpyAsync(M.ke0_dev.p, KeT, KE * sizeof(double), cudaMemcpyHostToDevice, c.stream));
     const double* ke0 = M.ke0_dev.as<double>();
+    // G_j = P_j^T Ke0 P_j for the 8 child positions j (SetupSolver.m:53-66 applied to one solid child)
+    static_assert(KE == 576, "24x24 element matrices");
+    std::vector<double> Gh(8 * KE, 0.0);
+    for (int j = 0; j < 8; ++j) {
+        const int dy = j & 1, dx = (j >> 1) & 1, dz = j >> 2;
+        double W[8][8];
+        for (int q = 0; q < 8; ++q)
+            for (int b = 0; b < 8; ++b) {
+                auto w1 = [](int pos, int c2) { const int d = pos > c2 ? pos - c2 : c2 - pos; return d == 0 ? 1.0 : (d == 1 ? 0.5 : 0.0); };
+                W[q][b] = w1(dy + corner_y(q), 2 * corner_y(b)) * w1(dx + corner_x(q), 2 * corner_x(b)) *
+                          w1(dz + corner_z(q), 2 * corner_z(b));
+            }
+        double T[KE];
+        for (int r = 0; r < 24; ++r)
+            for (int col = 0; col < 24; ++col) {
+                double v = 0;
+                for (int q = 0; q < 8; ++q) v += KeT[r * 24 + 3 * q + col % 3] * W[q][col / 3];
+                T[r * 24 + col] = v;
+            }
+        for (int row = 0; row < 24; ++row)
+            for (int col = 0; col < 24; ++col) {
+                double v = 0;
+                for (int p = 0; p < 8; ++p) v += W[p][row / 3] * T[(3 * p + row % 3) * 24 + col];
+                Gh[j * KE + row * 24 + col] = v;
+            }
+    }
+    M.galerkin_child = dalloc(8 * KE * sizeof(double));
+    GMGS_CUDA(cudaMemcpyAsync(M.galerkin_child.p, Gh.data(), 8 * KE * sizeof(double), cudaMemcpyHostToDevice, c.stream));
     // Galerkin matrices level by level
     for (int l = 1; l < L; ++l) {
         Level& lv = M.levels[l];
@@ -728,7 +729,8 @@ void build_operators(Model& M) {
         if (lv.nK > 0) {
             k_galerkin<<<(unsigned)lv.nK, 192, 0, c.stream>>>(
                 lv.g, fv.g, lv.kslot.as<int32_t>(), fv.emask.as<uint8_t>(), fv.etype.as<int32_t>(),
-                fv.Ks64.as<double>(), ke0, fv.kscale, l == 1 ? fv.escale64.as<double>() : nullptr,
+                fv.Ks64.as<double>(), M.galerkin_child.as<double>(), fv.kscale,
+                l == 1 ? fv.escale64.as<double>() : nullptr,
                 lv.Ks64.as<double>());
             GMGS_LAUNCHED(c);
         }

@@ -20,6 +20,7 @@ struct Model {
     bool own_stream = false;
     double ke0_rows[KE];   // Ke0 with row = output DOF
     DevBuf ke0_dev;
+    DevBuf galerkin_child; // 8 x 24x24: P_j^T Ke0 P_j per child position j
     DevBuf rho;            // compact density (double), extension
     // boundary conditions and solution (finest level, FP64, 3 planes)
     DevBuf F, U;
@@ -30,7 +31,7 @@ struct Model {
     // outer CG work vectors
     DevBuf cg_x, cg_r, cg_p, cg_dx, cg_q64, cg_y64, cg_z64;   // FP64 path
     DevBuf cg_q32, cg_y32, cg_z32, cg_r32;                     // mixed path
-    DevBuf cg_r32b, cg_pa, cg_pb, cg_dxp;                      // mixed path double buffers, pending dx
+    DevBuf cg_r32b, cg_pa, cg_pb;                              // mixed path double buffers
     Coef32 coef{};                                             // FP32 stencil + element matrix
     DevBuf scal;           // device scalars (see solver.cu)
     DevBuf dot_partials, dot_ticket;
@@ -48,7 +49,9 @@ DevBuf dalloc(size_t bytes);
 int64_t exclusive_scan(Ctx& c, int32_t* d, int64_t n);
 
 void element_stiffness(double E, double nu, const double ele[3], double Ke[KE]);
-void stress_matrices(double E, double nu, const double ele[3], double Mn[48 * 24], double Mg[48 * 24]);
+// Isotropic Hooke coefficients (d11, d12, d44) and reciprocal element edges
+// (1/dx, 1/dy, 1/dz) for the stress kernels.
+void stress_coefficients(double E, double nu, const double ele[3], double c[6]);
 
 // setup.cu
 void build_levels(Model& M, const int32_t* occ_dev);

@@ -74,6 +74,7 @@ SIGNATURES = {
     "gmgs_set_tolerance": (C.c_int, [_p, _d, _i32]),
     "gmgs_device_bytes": (C.c_int, [_p, _i64p]),
     "gmgs_launch_count": (C.c_int, [_p, _i64p]),
+    "gmgs_memory_stats": (C.c_int, [_i64p, _i64p, _i32]),
     "gmgs_phase_times": (C.c_int, [_p, _dp]),
     "gmgs_set_profiling": (C.c_int, [_p, _i32]),
     "gmgs_kernel_time": (C.c_int, [_p, _i32, _i64p, _dp, _dp]),

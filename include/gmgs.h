@@ -171,6 +171,10 @@ int gmgs_set_stream(gmgs_handle* h, void* cuda_stream);   /* cudaStream_t; NULL 
 int gmgs_set_tolerance(gmgs_handle* h, double tol, int32_t max_it);
 int gmgs_device_bytes(const gmgs_handle* h, int64_t* out);   /* device memory held by the handle */
 int gmgs_launch_count(const gmgs_handle* h, int64_t* out);   /* kernels launched so far */
+/* Device memory of all handles in the process (bytes now held, high-water mark
+ * since the last reset), including setup temporaries; reset_peak != 0 sets the
+ * mark to the current value after reading. */
+int gmgs_memory_stats(int64_t* current_bytes, int64_t* peak_bytes, int32_t reset_peak);
 int gmgs_phase_times(const gmgs_handle* h, double out[4]);   /* ms: create, bc-setup, last solve, last stress */
 /* Kernel timing with CUDA events on the handle's stream (diagnostics).
  * gmgs_set_profiling(h, 1) clears the records and starts recording;

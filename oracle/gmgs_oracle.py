@@ -748,11 +748,15 @@ class Oracle:
         Mn, Mg = stress_matrices(p.youngs_modulus, p.poisson_ratio, lv.eleSize)
         ue = self.U[lv.eDofMat]
         nodal_e = (ue @ Mn.T).reshape(-1, 8, 6)
+        per_voxel = (ue @ Mg.T).reshape(-1, 8, 6).mean(axis=1)
+        if self.rho is not None:          # extension: element stiffness rho^penal * Ke0
+            sc = self.rho ** self.penal
+            nodal_e = nodal_e * sc[:, None, None]
+            per_voxel = per_voxel * sc[:, None]
         out = np.zeros((lv.numNodes, 6))
         for k in range(8):
             out[lv.eNodMat[:, k]] += nodal_e[:, k]
         out /= self.numNod2Eles[:, None]
-        per_voxel = (ue @ Mg.T).reshape(-1, 8, 6).mean(axis=1)
         return out, per_voxel
 
     # ---------------- direct solve (test helper for gradient checks)

@@ -58,3 +58,17 @@ def test_compliance_gradient_is_negative():
     o, u = _solve(vox, fixed, loads, rho)
     g = o.gradient(u)
     assert np.all(g <= 1e-15)
+
+
+def test_stress_scales_with_uniform_density():
+    """Stress of a fixed displacement scales with a uniform rho^penal."""
+    vox, fixed, loads, rho = _model()
+    o, u = _solve(vox, fixed, loads, np.ones_like(rho))
+    o.U = u
+    n1, v1 = o.get_cartesian_stress()
+    o.set_density(np.full_like(rho, 0.5), 3.0)
+    o.setup()
+    o.U = u
+    n2, v2 = o.get_cartesian_stress()
+    assert np.allclose(n2, 0.125 * n1, rtol=1e-12, atol=1e-15)
+    assert np.allclose(v2, 0.125 * v1, rtol=1e-12, atol=1e-15)

@@ -1,7 +1,7 @@
 // Streaming FP32 operator kernels of the mixed-precision path.
 //
 // One CTA owns a 32 x 8 column of nodes (y fastest) and walks it through z
-// with a three-plane ring of the input field (plus a one-node halo) in shared
+// with a four-plane ring of the input field (plus a one-node halo) in shared
 // memory.  The field is formed while staging from the kernel's inputs (the
 // Jacobi step omega*D^-1 r, or the CG direction z + beta p), so no
 // intermediate vector goes through HBM.  The plane two steps ahead and the
@@ -36,6 +36,10 @@ constexpr int NT = TY * TX;
 constexpr int RP = 40;                  // shared-memory row pitch (>= HY; 8 mod 32 keeps 8x4 warp patches conflict-free)
 constexpr int PLANE = RP * HX;          // floats per component plane (34 x 10 points used)
 constexpr int NHALO = HY * HX - NT;     // 84 halo points per plane
+// Four ring slots need one barrier per plane: the slot written for plane z+1
+// in step z differs from the three slots (z-2, z-1, z) a thread still in step
+// z-1 may be reading.
+constexpr int RING = 4;
 
 // ---------------------------------------------------------------------------
 // host: assembled interior stencil from the element matrix (row = output DOF)
@@ -105,9 +109,12 @@ __device__ __forceinline__ void epi_fetch(const FineArgs& a, int S, int n, EpiDa
     }
 }
 
+// 64 registers (4 CTAs per SM) for the stencil-only modes; the CG update
+// holds FP64 state and keeps 80 registers (3 CTAs) without spilling.
 template <int MODE>
-__global__ void __launch_bounds__(NT, 3) k_fine(FineLevel L, const __grid_constant__ Coef32 cf, FineArgs a, int zc) {
-    __shared__ float ring[3][3 * PLANE];
+__global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? 3 : 4)
+    k_fine(FineLevel L, const __grid_constant__ Coef32 cf, FineArgs a, int zc) {
+    __shared__ float ring[RING][3 * PLANE];
     __shared__ double sh[32];
     const Grid& g = L.g;
     const int S = (int)g.slots;
@@ -155,9 +162,9 @@ __global__ void __launch_bounds__(NT, 3) k_fine(FineLevel L, const __grid_consta
 
     float vc[3], vh[3];
     fetch(zb - 1, vc, vh);
-    store(ring[(zb + 2) % 3], vc, vh);
+    store(ring[(zb - 1 + RING) % RING], vc, vh);
     fetch(zb, vc, vh);
-    store(ring[zb % 3], vc, vh);
+    store(ring[zb % RING], vc, vh);
     fetch(zb + 1, vc, vh);
 
     const bool own = cy <= g.ny && cx <= g.nx;
@@ -169,7 +176,7 @@ __global__ void __launch_bounds__(NT, 3) k_fine(FineLevel L, const __grid_consta
     Kahan dot;
 #pragma unroll 1
     for (int iz = zb; iz < ze; ++iz) {
-        store(ring[(iz + 1) % 3], vc, vh);
+        store(ring[(iz + 1) % RING], vc, vh);
         __syncthreads();
         if (iz + 2 <= g.nz + 1) fetch(iz + 2, vc, vh);
         const uint32_t f = f_next, e8 = e8_next;
@@ -177,9 +184,9 @@ __global__ void __launch_bounds__(NT, 3) k_fine(FineLevel L, const __grid_consta
             f_next = L.nflag[cbase + (iz + 1) * sz];
             e8_next = L.emask8[cbase + (iz + 1) * sz];
         }
-        const float* P0 = ring[(iz + 2) % 3];
-        const float* P1 = ring[iz % 3];
-        const float* P2 = ring[(iz + 1) % 3];
+        const float* P0 = ring[(iz - 1 + RING) % RING];
+        const float* P1 = ring[iz % RING];
+        const float* P2 = ring[(iz + 1) % RING];
         if (own && (f & NF_SOLID) && !(f & NF_PEREL)) {
             const int n = cbase + iz * sz;
             EpiData ed;
@@ -226,14 +233,13 @@ __global__ void __launch_bounds__(NT, 3) k_fine(FineLevel L, const __grid_consta
                 }
             }
         }
-        __syncthreads();
     }
     if (MODE == FM_CG_DIRECTION || MODE == FM_CG_UPDATE_JACOBI) grid_dot_finish(dot.value(), a.dot, sh);
 }
 
 static int pick_zc(const Grid& g, const Ctx& c) {
     const int64_t cols = (int64_t)((g.ny + 1 + TY - 1) / TY) * ((g.nx + 1 + TX - 1) / TX);
-    const int64_t want = (int64_t)c.num_sms * 3 * 6;      // ~6 waves of resident CTAs
+    const int64_t want = (int64_t)c.num_sms * 3 * 12;     // ~12 waves of resident CTAs
     int64_t zc = (cols * (g.nz + 1) + want - 1) / want;
     if (zc < 4) zc = 4;
     if (zc > 64) zc = 64;

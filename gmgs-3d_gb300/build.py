@@ -20,7 +20,9 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = ROOT / "_build" / "gmgs"
 LIB = PKG / "gmgs" / "libgmgs.so"
-SOURCES = ["api.cu", "setup.cu", "operators.cu", "solver.cu", "post.cu", "fine.cu", "noalloc.cu"]
+SOURCES = ["api.cu", "setup.cu", "operators.cu", "solver.cu", "post.cu", "fine.cu", "noalloc.cu", "voxelize.cu"]
+# the voxeliser decides inside/outside by exact FP64 comparisons: no FMA contraction
+FILE_FLAGS = {"voxelize.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -44,7 +46,7 @@ def compile_one(src: str, debug: bool) -> Path:
     deps = [srcp] + list(CSRC.glob("*.cuh")) + [ROOT / "include" / "gmgs.h"]
     if out.exists() and all(out.stat().st_mtime >= d.stat().st_mtime for d in deps) and not debug:
         return out
-    cmd = [nvcc(), *flags(debug), "-c", str(srcp), "-o", str(out)]
+    cmd = [nvcc(), *flags(debug), *FILE_FLAGS.get(src, []), "-c", str(srcp), "-o", str(out)]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src}:\n{res.stdout}\n{res.stderr}")

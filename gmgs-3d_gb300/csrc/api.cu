@@ -156,6 +156,7 @@ const char* gmgs_status_string(int s) {
         case GMGS_ERR_CUDA: return "CUDA error";
         case GMGS_ERR_OUT_OF_MEMORY: return "out of device memory";
         case GMGS_ERR_STATE: return "call order";
+        case GMGS_ERR_MESH: return "mesh not voxelisable";
         default: return "unknown status";
     }
 }

@@ -25,6 +25,7 @@ ERR_NO_SOLUTION = 9
 ERR_CUDA = 10
 ERR_OUT_OF_MEMORY = 11
 ERR_STATE = 12
+ERR_MESH = 13
 
 FP64 = 0
 MIXED = 1
@@ -74,6 +75,7 @@ SIGNATURES = {
     "gmgs_set_tolerance": (C.c_int, [_p, _d, _i32]),
     "gmgs_device_bytes": (C.c_int, [_p, _i64p]),
     "gmgs_launch_count": (C.c_int, [_p, _i64p]),
+    "gmgs_voxelize_mesh": (C.c_int, [_dp, _i64, _i32p, _i64, _i32, _i32p, _i32p]),
     "gmgs_memory_stats": (C.c_int, [_i64p, _i64p, _i32]),
     "gmgs_phase_times": (C.c_int, [_p, _dp]),
     "gmgs_set_profiling": (C.c_int, [_p, _i32]),

@@ -282,9 +282,24 @@ class Session:
         self.iterationHist_ = np.zeros((0, 3))
         self._solver = None
 
-    def CreateVoxilizedModel(self, nx, ny, nz):
-        """Solid cuboid overload (src/common/CreateVoxilizedModel.m:27-32)."""
-        self.voxelizedVolume_ = np.ones((ny, nx, nz), dtype=np.int32)
+    def CreateVoxilizedModel(self, *args):
+        """CreateVoxilizedModel(triFaceModelFile, finestResCtrl): voxelise an
+        ASCII .ply mesh on the GPU (src/common/CreateVoxilizedModel.m:10-26);
+        the voxel edge lengths follow from the mesh bounding box
+        (DiscretizeDesignDomain.m:53-65).
+        CreateVoxilizedModel(nx, ny, nz): solid cuboid of unit voxels (:27-32)."""
+        if len(args) == 2:
+            from . import mesh
+            vertices, faces = mesh.read_ply(args[0])
+            self.voxelizedVolume_, ele = mesh.voxelize(vertices, faces, int(args[1]))
+            self.eleSize_ = tuple(float(e) for e in ele)
+        elif len(args) == 3:
+            nx, ny, nz = (int(a) for a in args)
+            self.voxelizedVolume_ = np.ones((ny, nx, nz), dtype=np.int32)
+            self.eleSize_ = (1.0, 1.0, 1.0)
+        else:
+            raise GMGSError(L.ERR_INVALID_ARGUMENT, "Wrong input for voxelization!")
+        self._solver = None
         return self.voxelizedVolume_
 
     def DiscretizeDesignDomain(self):

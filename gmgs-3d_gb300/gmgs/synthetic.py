@@ -157,3 +157,62 @@ def make(workload: Workload | str, scale: float = 1.0):
     if w.rho_range is not None:
         rho = density(int(vox.sum()), w.rho_range, w.seed)
     return vox, fixed, loads, L, rho
+
+
+# ---------------------------------------------------------------------------
+# closed triangle meshes for the voxeliser (synthetic stand-ins for the
+# reference's kitten and parts models)
+# ---------------------------------------------------------------------------
+def blob_mesh(n_lat: int = 24, n_lon: int = 48, seed: int = 0, amp: float = 0.25):
+    """(vertices, faces) of a closed genus-0 surface: a UV sphere whose radius
+    varies with a few seeded low-order harmonics.  Outward-oriented faces."""
+    rng = np.random.default_rng(seed)
+    coef = rng.normal(size=(4, 4)) * amp / 4
+    phase = rng.uniform(0, 2 * np.pi, size=(4, 4))
+    th = np.linspace(0, np.pi, n_lat + 1)[1:-1]
+    ph = np.linspace(0, 2 * np.pi, n_lon, endpoint=False)
+    T, P = np.meshgrid(th, ph, indexing="ij")
+
+    def radius(t, p):
+        r = np.ones_like(t)
+        for i in range(4):
+            for j in range(4):
+                r = r + coef[i, j] * np.cos((i + 1) * t) * np.cos(j * p + phase[i, j])
+        return r
+
+    R = radius(T, P)
+    ring = np.stack([R * np.sin(T) * np.cos(P), R * np.sin(T) * np.sin(P), R * np.cos(T)], axis=-1).reshape(-1, 3)
+    north = np.array([[0.0, 0.0, float(radius(np.zeros(1), np.zeros(1))[0])]])
+    south = np.array([[0.0, 0.0, -float(radius(np.full(1, np.pi), np.zeros(1))[0])]])
+    verts = np.concatenate([north, ring, south]) * np.array([1.3, 1.0, 1.6]) + 3.0
+    nn, ns = 0, 1 + ring.shape[0]
+    vid = lambda i, j: 1 + i * n_lon + (j % n_lon)
+    faces = []
+    for j in range(n_lon):
+        faces.append((nn, vid(0, j), vid(0, j + 1)))
+        faces.append((ns, vid(n_lat - 2, j + 1), vid(n_lat - 2, j)))
+    for i in range(n_lat - 2):
+        for j in range(n_lon):
+            a, b, c, d = vid(i, j), vid(i, j + 1), vid(i + 1, j), vid(i + 1, j + 1)
+            faces.append((a, c, b))
+            faces.append((b, c, d))
+    return verts, np.asarray(faces, dtype=np.int32)
+
+
+def torus_mesh(R: float = 2.0, r: float = 0.7, nu: int = 48, nv: int = 24, seed: int = 0):
+    """(vertices, faces) of a closed torus (genus 1) with seeded vertex jitter."""
+    rng = np.random.default_rng(seed)
+    u = np.linspace(0, 2 * np.pi, nu, endpoint=False)
+    v = np.linspace(0, 2 * np.pi, nv, endpoint=False)
+    U, V = np.meshgrid(u, v, indexing="ij")
+    rr = r * (1 + 0.05 * rng.standard_normal(U.shape))
+    verts = np.stack([(R + rr * np.cos(V)) * np.cos(U), (R + rr * np.cos(V)) * np.sin(U), rr * np.sin(V)],
+                     axis=-1).reshape(-1, 3) + np.array([3.0, 3.0, 1.0])
+    vid = lambda i, j: (i % nu) * nv + (j % nv)
+    faces = []
+    for i in range(nu):
+        for j in range(nv):
+            a, b, c, d = vid(i, j), vid(i + 1, j), vid(i, j + 1), vid(i + 1, j + 1)
+            faces.append((a, b, d))
+            faces.append((a, d, c))
+    return verts, np.asarray(faces, dtype=np.int32)

@@ -47,7 +47,8 @@ enum gmgs_status {
     GMGS_ERR_NO_SOLUTION = 9,       /* stress/gradient before a solve: GetCartesianStress.m:7-9 */
     GMGS_ERR_CUDA = 10,             /* CUDA runtime or cuSOLVER failure */
     GMGS_ERR_OUT_OF_MEMORY = 11,
-    GMGS_ERR_STATE = 12             /* call order (e.g. solve before set_bc) */
+    GMGS_ERR_STATE = 12,            /* call order (e.g. solve before set_bc) */
+    GMGS_ERR_MESH = 13              /* a mesh the reference's voxeliser cannot handle (Voxelize.m:176-203) */
 };
 
 enum gmgs_precision {
@@ -82,6 +83,20 @@ void gmgs_default_params(gmgs_params* p);
  * (DiscretizeDesignDomain.m:65). */
 int gmgs_create(const int32_t* occupancy, int32_t ny, int32_t nx, int32_t nz,
                 const double ele_size[3], const gmgs_params* params, gmgs_handle** out);
+
+/* Mesh voxelisation; replaces CreateVoxilizedModel(triFaceModelFile,
+ * finestResCtrl) (src/common/CreateVoxilizedModel.m:10-26 with
+ * AdaptData4Voxelize.m:5-18 and Voxelize.m:1-331): the longest bounding-box
+ * side gets finest_resolution voxels, rays along x, y and z through the voxel
+ * centres decide inside/outside by crossing parity, a voxel is solid when two
+ * of the three directions agree, and the result is flipped along y.
+ * vertices: nv x 3 (x, y, z) row-major; faces: nf x 3 0-based vertex ids.
+ * dims receives {ny, nx, nz}; with occupancy == NULL only dims are computed,
+ * otherwise occupancy (ny*nx*nz int32, y fastest, 1 = solid) is filled.
+ * The voxel edge lengths for gmgs_create are the bounding-box extents divided
+ * by {nx, ny, nz} (DiscretizeDesignDomain.m:53-65). */
+int gmgs_voxelize_mesh(const double* vertices, int64_t nv, const int32_t* faces, int64_t nf,
+                       int32_t finest_resolution, int32_t dims[3], int32_t* occupancy);
 
 /* Boundary conditions; replaces ApplyBoundaryCondition()
  * (src/common/ApplyBoundaryCondition.m:1-24) with fixingCond_ / loadingCond_.

@@ -40,9 +40,10 @@ CLOCK_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.a
 
 
 # DRAM bytes (read + write) per solid node of one k_fine<FM_CG_UPDATE_JACOBI>
-# launch, from an ncu capture of the same kernel at half resolution (the
-# traffic grows with the node count); None until measured.
-UJ_TRAFFIC_PER_NODE = None
+# launch: 1,122,968,576 B over 6,360,481 nodes in an ncu --set full capture of
+# the same kernel on the same generator at half resolution (--scale 0.5); the
+# traffic grows with the node count.
+UJ_TRAFFIC_PER_NODE = 176.6
 
 
 def parse():
@@ -58,6 +59,14 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle sample")
     ap.add_argument("--cpu-scale", type=float, default=0.125)
+    # a real mesh instead of the synthetic workload: the reference's demo inputs
+    # (data/<model>.ply, data/demo_BC_<model>_<res>_fixedNodes.dat / _loadingVec.dat)
+    ap.add_argument("--mesh", default=None, help="ASCII .ply triangle mesh (CreateVoxilizedModel input)")
+    ap.add_argument("--res", type=int, default=512, help="finestResolutionControl_ for --mesh")
+    ap.add_argument("--fixed", default=None, help="fixingCond_ file (node ids) for --mesh")
+    ap.add_argument("--loads", default=None, help="loadingCond_ file (id fx fy fz rows) for --mesh")
+    ap.add_argument("--published-s", type=float, default=None,
+                    help="published seconds for this model (vs_baseline = value / published)")
     return ap.parse_args()
 
 
@@ -385,10 +394,74 @@ def run_gmgs(a):
     s.close()
 
 
+def run_mesh(a):
+    """The reference's own demo flow (Demo.m:67-77) on one GPU: voxelise the
+    mesh, discretise, apply the demo boundary conditions, solve to tol 1e-3
+    with the reference's default controls (omega 0.4, the level rule), in the
+    mixed and the FP64 path.  `value` is the mixed solve on device-resident
+    data; `e2e` runs from the host mesh and boundary-condition arrays to U on
+    the host."""
+    import numpy as np
+    import torch
+    from gmgs import Solver, mesh as M
+
+    v, f = M.read_ply(a.mesh)
+    fixed = np.loadtxt(a.fixed, ndmin=1).astype(np.int32)
+    loads = np.loadtxt(a.loads, ndmin=2)
+    stream = torch.cuda.Stream()
+    res = {}
+    for prec in ("mixed", "fp64"):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        vol, ele = M.voxelize(v, f, a.res)
+        t1 = time.perf_counter()
+        s = Solver(vol, ele_size=ele, precision=prec)
+        s.set_bc(fixed, loads)
+        u = s.solve()
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        s.set_stream(stream.cuda_stream)
+        k = a.steps if prec == "mixed" else 1
+        for _ in range(a.warmup if prec == "mixed" else 0):
+            s.solve_dev(None)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        with ClockSampler(0) as clk:
+            e0.record(stream)
+            for _ in range(k):
+                s.solve_dev(None)
+            e1.record(stream)
+            torch.cuda.synchronize()
+        res[prec] = {"solve_s": e0.elapsed_time(e1) / k / 1e3, "e2e_s": t2 - t0, "voxelize_s": t1 - t0,
+                     "iterations": s.iterations, "relres": s.relres, "u": u, "dofs": 3 * s.num_nodes(1),
+                     "levels": s.num_levels, "phases_ms": s.phase_times_ms, "device_bytes": s.device_bytes,
+                     "clocks": clk.summary(), "grid": list(vol.shape)}
+        s.close()
+    mx, fp = res["mixed"], res["fp64"]
+    err = float(np.linalg.norm(mx["u"] - fp["u"]) / np.linalg.norm(fp["u"]))
+    line = {
+        "metric": METRIC + " (reference demo mesh)", "value": mx["solve_s"], "unit": "s", "n_gpus": 1,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": mx["solve_s"] * 1e3, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": (mx["solve_s"] / a.published_s) if a.published_s else None,
+        "dtype": "f32 V-cycle / f64 CG", "data": f"mesh {Path(a.mesh).name} with its demo boundary conditions",
+        "config": {"workload": f"{Path(a.mesh).stem}_{a.res}", "grid_ny_nx_nz": mx["grid"], "dofs": mx["dofs"],
+                   "levels": mx["levels"], "omega": 0.4, "tol": 1e-3, "iterations": mx["iterations"],
+                   "relres": mx["relres"], "published_s": a.published_s},
+        "e2e": {"value": mx["e2e_s"], "unit": "s", "voxelize_s": mx["voxelize_s"], "phases_ms": mx["phases_ms"]},
+        "fp64": {"seconds": fp["solve_s"], "e2e_s": fp["e2e_s"], "iterations": fp["iterations"],
+                 "relres": fp["relres"], "speedup_mixed_vs_fp64": fp["solve_s"] / mx["solve_s"],
+                 "displacement_rel_err_mixed_vs_fp64": err},
+        "clocks": mx["clocks"], "device_bytes": mx["device_bytes"],
+    }
+    print(json.dumps(line))
+
+
 def main():
     a = parse()
     if a.impl == "reference":
         run_reference(a)
+    elif a.mesh:
+        run_mesh(a)
     else:
         run_gmgs(a)
 

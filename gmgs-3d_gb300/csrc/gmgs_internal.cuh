@@ -265,7 +265,7 @@ template <typename T>
 void launch_gather(Ctx& c, int64_t n, const int32_t* idx, const T* src, double* dst);
 template <typename T>
 void launch_scatter(Ctx& c, int64_t n, const int32_t* idx, const double* src, T* dst);
-void launch_gemv(Ctx& c, int n, const double* A, const double* x, double* y);
+void launch_coarse_solve(Ctx& c, int n, const double* kinv, const double* r, double* tmp, double* z);
 
 // compact <-> dense (interleaved 3-vectors)
 template <typename T>

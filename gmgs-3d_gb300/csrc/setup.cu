@@ -862,20 +862,27 @@ void build_coarse_bc(Model& M) {
         lc.g, (int)nf, M.free_idx.as<int32_t>(), rank.as<int32_t>(), lc.emask.as<uint8_t>(), lc.etype.as<int32_t>(),
         lc.Ks64.as<double>(), M.ke0_dev.as<double>(), lc.kscale, M.kinv.as<double>());
     GMGS_LAUNCHED(c);
-    // Kd is row-major K[row][col]; cuSOLVER is column-major, so it sees K^T.
-    // potrf/potri read the lower triangle of what they see.
+    // Kd is row-major K[row][col]; cuSOLVER is column-major, so it sees K^T = K.
+    // potrf factors K = L L^T into the column-major lower triangle and trtri
+    // replaces L by Linv = L^-1 there (row-major: the upper triangle holds
+    // Linv^T).  Mirroring it into the row-major lower triangle gives
+    //   kinv[i][j] = Linv[i][j] (j <= i),  kinv[i][j] = Linv[j][i] (j >= i),
+    // so K^-1 r = Linv^T (Linv r) is two half-row sweeps (launch_coarse_solve).
+    // Forming Linv instead of K^-1 (potri) skips the L^-T L^-1 product.
     cusolverDnHandle_t hs = nullptr;
     if (cusolverDnCreate(&hs) != CUSOLVER_STATUS_SUCCESS) throw Error(GMGS_ERR_CUDA, "cusolverDnCreate failed");
     struct Guard { cusolverDnHandle_t h; ~Guard() { cusolverDnDestroy(h); } } guard{hs};
     cusolverDnSetStream(hs, c.stream);
-    int lwork = 0, lwork2 = 0;
+    int lwork = 0;
+    size_t tw_dev = 0, tw_host = 0;
     const int n = (int)nf;
     if (cusolverDnDpotrf_bufferSize(hs, CUBLAS_FILL_MODE_LOWER, n, M.kinv.as<double>(), n, &lwork) !=
             CUSOLVER_STATUS_SUCCESS ||
-        cusolverDnDpotri_bufferSize(hs, CUBLAS_FILL_MODE_LOWER, n, M.kinv.as<double>(), n, &lwork2) !=
-            CUSOLVER_STATUS_SUCCESS)
+        cusolverDnXtrtri_bufferSize(hs, CUBLAS_FILL_MODE_LOWER, CUBLAS_DIAG_NON_UNIT, n, CUDA_R_64F, M.kinv.p, n,
+                                    &tw_dev, &tw_host) != CUSOLVER_STATUS_SUCCESS)
         throw Error(GMGS_ERR_CUDA, "cuSOLVER buffer size query failed");
-    DevBuf work = dalloc((size_t)std::max(lwork, lwork2) * sizeof(double));
+    DevBuf work = dalloc(std::max((size_t)lwork * sizeof(double), tw_dev));
+    std::vector<unsigned char> hwork(std::max<size_t>(1, tw_host));
     DevBuf info = dalloc(sizeof(int));
     if (cusolverDnDpotrf(hs, CUBLAS_FILL_MODE_LOWER, n, M.kinv.as<double>(), n, work.as<double>(), lwork,
                          info.as<int>()) != CUSOLVER_STATUS_SUCCESS)
@@ -884,14 +891,15 @@ void build_coarse_bc(Model& M) {
     GMGS_CUDA(cudaMemcpyAsync(&hinfo, info.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
     GMGS_CUDA(cudaStreamSynchronize(c.stream));
     if (hinfo != 0) throw Error(GMGS_ERR_NOT_SPD, "coarsest-level matrix is not positive definite");
-    if (cusolverDnDpotri(hs, CUBLAS_FILL_MODE_LOWER, n, M.kinv.as<double>(), n, work.as<double>(), lwork2,
-                         info.as<int>()) != CUSOLVER_STATUS_SUCCESS)
-        throw Error(GMGS_ERR_CUDA, "cusolverDnDpotri failed");
+    if (cusolverDnXtrtri(hs, CUBLAS_FILL_MODE_LOWER, CUBLAS_DIAG_NON_UNIT, n, CUDA_R_64F, M.kinv.p, n, work.p, tw_dev,
+                         hwork.data(), tw_host, info.as<int>()) != CUSOLVER_STATUS_SUCCESS)
+        throw Error(GMGS_ERR_CUDA, "cusolverDnXtrtri failed");
     GMGS_CUDA(cudaMemcpyAsync(&hinfo, info.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
     GMGS_CUDA(cudaStreamSynchronize(c.stream));
-    if (hinfo != 0) throw Error(GMGS_ERR_NOT_SPD, "coarsest-level inverse failed");
+    if (hinfo != 0) throw Error(GMGS_ERR_NOT_SPD, "coarsest-level factor is singular");
     k_symmetrize_lower<<<blocks_for(c, (int64_t)n * n), 256, 0, c.stream>>>(n, M.kinv.as<double>());
     GMGS_LAUNCHED(c);
+    M.cvec_tmp = dalloc(nf * sizeof(double));
     M.cvec_in = dalloc(nf * sizeof(double));
     M.cvec_out = dalloc(nf * sizeof(double));
     GMGS_CUDA(cudaStreamSynchronize(c.stream));

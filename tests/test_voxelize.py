@@ -178,7 +178,7 @@ def test_session_mesh_overload(tmp_path):
         fh.write(f"ply\nformat ascii 1.0\nelement vertex {len(v)}\nproperty float x\nproperty float y\n"
                  f"property float z\nelement face {len(f)}\nproperty list uchar int vertex_indices\nend_header\n")
         for x in v:
-            fh.write(f"{x[0]!r} {x[1]!r} {x[2]!r}\n")
+            fh.write(f"{float(x[0])!r} {float(x[1])!r} {float(x[2])!r}\n")
         for t in f:
             fh.write(f"3 {t[0]} {t[1]} {t[2]}\n")
     s = Session()

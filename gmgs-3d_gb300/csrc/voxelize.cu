@@ -10,8 +10,8 @@
 // and a voxel is solid when at least two directions agree.  The result is
 // flipped along y (CreateVoxilizedModel.m:21).
 //
-// One thread per ray; each ray only tests the facets whose extent along the
-// ray row's coordinate covers it (a CSR list per row built on the host).
+// One thread per ray; each ray only tests the facets whose bounding box
+// covers it (per-ray candidate lists built on the host).
 // The decisions are exact comparisons of FP64 expressions, so this file is
 // compiled without FMA contraction (device: -fmad=false, host:
 // -ffp-contract=off) and evaluates every expression in the reference's
@@ -88,7 +88,8 @@ struct RayArgs {
     const double *gx, *gy, *gz;
     int nx, ny, nz;
     int ix0, ix1, iy0, iy1;               // ray window (inclusive)
-    const int32_t *row_ptr, *row_fac;     // candidate facets of row iy - iy0
+    const int64_t* ray_ptr;               // candidate facets of window ray t: ray_fac[ray_ptr[t] .. ray_ptr[t+1])
+    const int32_t* ray_fac;
     double zlo, zhi;                      // mesh z limits with the 1e-12 margin
     uint8_t* out;                         // [ix][iy][iz]
     uint8_t* odd;                         // [ix][iy]
@@ -108,8 +109,8 @@ __global__ void __launch_bounds__(128) k_rays(RayArgs a) {
     const int64_t m = a.m;
     double zs[MAXC];
     int nzc = 0;
-    for (int k = a.row_ptr[iy - a.iy0]; k < a.row_ptr[iy - a.iy0 + 1]; ++k) {
-        const int f = a.row_fac[k];
+    for (int64_t k = a.ray_ptr[t]; k < a.ray_ptr[t + 1]; ++k) {
+        const int f = a.ray_fac[k];
         if (!(F[FMINX * m + f] <= xv && F[FMAXX * m + f] >= xv)) continue;
         const double x1 = F[X1 * m + f], x2 = F[X2 * m + f], x3 = F[X3 * m + f];
         const double y1 = F[Y1 * m + f], y2 = F[Y2 * m + f], y3 = F[Y3 * m + f];
@@ -156,25 +157,23 @@ __global__ void __launch_bounds__(128) k_rays(RayArgs a) {
 
 // rays with an odd number of crossings, in the order the reference records
 // them (y outer, x inner): the voxel is inside when >= 4 of the 8
-// neighbouring rays have it inside (Voxelize.m:306-330); one thread, since
-// later corrections see earlier ones
-__global__ void k_correct(uint8_t* out, const uint8_t* odd, int nx, int ny, int nz, int ix0, int ix1, int iy0,
-                          int iy1) {
-    if (blockIdx.x != 0 || threadIdx.x != 0) return;
-    for (int iy = iy0; iy <= iy1; ++iy)
-        for (int ix = ix0; ix <= ix1; ++ix) {
-            if (!odd[(int64_t)ix * ny + iy]) continue;
-            for (int k = 0; k < nz; ++k) {
-                int s = 0;
-                for (int dx = -1; dx <= 1; ++dx)
-                    for (int dy = -1; dy <= 1; ++dy) {
-                        if (!dx && !dy) continue;
-                        const int jx = ix + dx, jy = iy + dy;
-                        if (jx >= 0 && jx < nx && jy >= 0 && jy < ny) s += out[((int64_t)jx * ny + jy) * nz + k];
-                    }
-                if (s >= 4) out[((int64_t)ix * ny + iy) * nz + k] = 1;
+// neighbouring rays have it inside (Voxelize.m:306-330).  A correction reads
+// and writes one z position only, so every z position is an independent
+// sequence: one thread per z walks the ordered list.
+__global__ void k_correct(uint8_t* out, const int32_t* __restrict__ odd_xy, int n_odd, int nx, int ny, int nz) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nz) return;
+    for (int c = 0; c < n_odd; ++c) {
+        const int ix = odd_xy[2 * c], iy = odd_xy[2 * c + 1];
+        int s = 0;
+        for (int dx = -1; dx <= 1; ++dx)
+            for (int dy = -1; dy <= 1; ++dy) {
+                if (!dx && !dy) continue;
+                const int jx = ix + dx, jy = iy + dy;
+                if (jx >= 0 && jx < nx && jy >= 0 && jy < ny) s += out[((int64_t)jx * ny + jy) * nz + k];
             }
-        }
+        if (s >= 4) out[((int64_t)ix * ny + iy) * nz + k] = 1;
+    }
 }
 
 // majority of the three directions, permuted to (y, x, z) and flipped in y
@@ -218,49 +217,68 @@ void ray_direction(const std::vector<double>& mesh, int64_t m, int au, int av, i
     int ix0 = nearest(gu, umin), ix1 = nearest(gu, umax), iy0 = nearest(gv, vmin), iy1 = nearest(gv, vmax);
     if (ix0 > ix1) std::swap(ix0, ix1);
     if (iy0 > iy1) std::swap(iy0, iy1);
-    // candidate facets per ray row (Voxelize.m:144): min_v <= gv[iy] <= max_v
-    const int rows = iy1 - iy0 + 1;
-    std::vector<int32_t> cnt(rows + 1, 0);
-    auto row_range = [&](int64_t f, int& lo, int& hi) {
-        lo = (int)(std::lower_bound(gv.begin() + iy0, gv.begin() + iy1 + 1, fvmin[f]) - gv.begin());
-        hi = (int)(std::upper_bound(gv.begin() + iy0, gv.begin() + iy1 + 1, fvmax[f]) - gv.begin()) - 1;
-    };
+    // candidate facets per ray (Voxelize.m:144-150): min_v <= gv[iy] <= max_v and
+    // min_u <= gu[ix] <= max_u, binned by each facet's bounding box
+    const int wx = ix1 - ix0 + 1, rows = iy1 - iy0 + 1;
+    const int64_t nrays = (int64_t)wx * rows;
+    std::vector<int64_t> ptr(nrays + 1, 0);
+    std::vector<int> blo(4 * m);
     for (int64_t f = 0; f < m; ++f) {
-        int lo, hi;
-        row_range(f, lo, hi);
-        for (int r = lo; r <= hi; ++r) ++cnt[r - iy0 + 1];
+        const double fumin = std::min(std::min(F[X1 * m + f], F[X2 * m + f]), F[X3 * m + f]);
+        const double fumax = std::max(std::max(F[X1 * m + f], F[X2 * m + f]), F[X3 * m + f]);
+        int* b = &blo[4 * f];
+        b[0] = (int)(std::lower_bound(gu.begin() + ix0, gu.begin() + ix1 + 1, fumin) - gu.begin());
+        b[1] = (int)(std::upper_bound(gu.begin() + ix0, gu.begin() + ix1 + 1, fumax) - gu.begin()) - 1;
+        b[2] = (int)(std::lower_bound(gv.begin() + iy0, gv.begin() + iy1 + 1, fvmin[f]) - gv.begin());
+        b[3] = (int)(std::upper_bound(gv.begin() + iy0, gv.begin() + iy1 + 1, fvmax[f]) - gv.begin()) - 1;
+        for (int iy = b[2]; iy <= b[3]; ++iy)
+            for (int ix = b[0]; ix <= b[1]; ++ix) ++ptr[(int64_t)(iy - iy0) * wx + (ix - ix0) + 1];
     }
-    for (int r = 0; r < rows; ++r) cnt[r + 1] += cnt[r];
-    if (cnt[rows] > INT32_MAX / 2) throw Error(GMGS_ERR_INVALID_ARGUMENT, "mesh too large for the row lists");
-    std::vector<int32_t> fac(std::max<int32_t>(1, cnt[rows]));
-    std::vector<int32_t> pos(cnt.begin(), cnt.end() - 1);
-    for (int64_t f = 0; f < m; ++f) {
-        int lo, hi;
-        row_range(f, lo, hi);
-        for (int r = lo; r <= hi; ++r) fac[pos[r - iy0]++] = (int32_t)f;
+    for (int64_t r = 0; r < nrays; ++r) ptr[r + 1] += ptr[r];
+    std::vector<int32_t> fac(std::max<int64_t>(1, ptr[nrays]));
+    {
+        std::vector<int64_t> pos(ptr.begin(), ptr.end() - 1);
+        for (int64_t f = 0; f < m; ++f) {
+            const int* b = &blo[4 * f];
+            for (int iy = b[2]; iy <= b[3]; ++iy)
+                for (int ix = b[0]; ix <= b[1]; ++ix) fac[pos[(int64_t)(iy - iy0) * wx + (ix - ix0)]++] = (int32_t)f;
+        }
     }
     DevBuf dF = dalloc(F.size() * sizeof(double)), dgu = dalloc(nu * sizeof(double)), dgv = dalloc(nv * sizeof(double)),
-           dgw = dalloc(nw * sizeof(double)), dptr = dalloc(cnt.size() * sizeof(int32_t)),
+           dgw = dalloc(nw * sizeof(double)), dptr = dalloc(ptr.size() * sizeof(int64_t)),
            dfac = dalloc(fac.size() * sizeof(int32_t)), dodd = dalloc((size_t)nu * nv);
     out = dalloc((size_t)nu * nv * nw);
     GMGS_CUDA(cudaMemcpyAsync(dF.p, F.data(), F.size() * sizeof(double), cudaMemcpyHostToDevice, st));
     GMGS_CUDA(cudaMemcpyAsync(dgu.p, gu.data(), nu * sizeof(double), cudaMemcpyHostToDevice, st));
     GMGS_CUDA(cudaMemcpyAsync(dgv.p, gv.data(), nv * sizeof(double), cudaMemcpyHostToDevice, st));
     GMGS_CUDA(cudaMemcpyAsync(dgw.p, gw.data(), nw * sizeof(double), cudaMemcpyHostToDevice, st));
-    GMGS_CUDA(cudaMemcpyAsync(dptr.p, cnt.data(), cnt.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    GMGS_CUDA(cudaMemcpyAsync(dptr.p, ptr.data(), ptr.size() * sizeof(int64_t), cudaMemcpyHostToDevice, st));
     GMGS_CUDA(cudaMemcpyAsync(dfac.p, fac.data(), fac.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
     GMGS_CUDA(cudaMemsetAsync(out.p, 0, (size_t)nu * nv * nw, st));
     GMGS_CUDA(cudaMemsetAsync(dodd.p, 0, (size_t)nu * nv, st));
     k_facet_prep<<<(unsigned)std::min<int64_t>((m + 255) / 256, 4096), 256, 0, st>>>(m, dF.as<double>());
     GMGS_CUDA(cudaGetLastError());
     RayArgs a{dF.as<double>(), m, dgu.as<double>(), dgv.as<double>(), dgw.as<double>(), nu, nv, nw, ix0, ix1, iy0, iy1,
-              dptr.as<int32_t>(), dfac.as<int32_t>(), wmin - 1e-12, wmax + 1e-12, out.as<uint8_t>(),
+              dptr.as<int64_t>(), dfac.as<int32_t>(), wmin - 1e-12, wmax + 1e-12, out.as<uint8_t>(),
               dodd.as<uint8_t>(), dflags.as<int>()};
-    const int64_t rays = (int64_t)(ix1 - ix0 + 1) * rows;
-    k_rays<<<(unsigned)((rays + 127) / 128), 128, 0, st>>>(a);
+    k_rays<<<(unsigned)((nrays + 127) / 128), 128, 0, st>>>(a);
     GMGS_CUDA(cudaGetLastError());
-    k_correct<<<1, 1, 0, st>>>(out.as<uint8_t>(), dodd.as<uint8_t>(), nu, nv, nw, ix0, ix1, iy0, iy1);
-    GMGS_CUDA(cudaGetLastError());
+    // the odd rays in the reference's order (y outer, x inner)
+    std::vector<uint8_t> odd((size_t)nu * nv);
+    GMGS_CUDA(cudaMemcpyAsync(odd.data(), dodd.p, odd.size(), cudaMemcpyDeviceToHost, st));
+    GMGS_CUDA(cudaStreamSynchronize(st));
+    std::vector<int32_t> odd_xy;
+    for (int iy = iy0; iy <= iy1; ++iy)
+        for (int ix = ix0; ix <= ix1; ++ix)
+            if (odd[(size_t)ix * nv + iy]) { odd_xy.push_back(ix); odd_xy.push_back(iy); }
+    if (!odd_xy.empty()) {
+        DevBuf dxy = dalloc(odd_xy.size() * sizeof(int32_t));
+        GMGS_CUDA(cudaMemcpyAsync(dxy.p, odd_xy.data(), odd_xy.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+        k_correct<<<(nw + 127) / 128, 128, 0, st>>>(out.as<uint8_t>(), dxy.as<int32_t>(), (int)(odd_xy.size() / 2), nu,
+                                                   nv, nw);
+        GMGS_CUDA(cudaGetLastError());
+        GMGS_CUDA(cudaStreamSynchronize(st));
+    }
     GMGS_CUDA(cudaStreamSynchronize(st));   // host vectors and temporaries go out of scope
 }
 

@@ -280,6 +280,7 @@ class Session:
         self.U_ = None
         self.cartesianStressField_ = None
         self.iterationHist_ = np.zeros((0, 3))
+        self.boundingBox_ = None
         self._solver = None
 
     def CreateVoxilizedModel(self, *args):
@@ -293,10 +294,12 @@ class Session:
             vertices, faces = mesh.read_ply(args[0])
             self.voxelizedVolume_, ele = mesh.voxelize(vertices, faces, int(args[1]))
             self.eleSize_ = tuple(float(e) for e in ele)
+            self.boundingBox_ = np.stack([vertices.min(axis=0), vertices.max(axis=0)])
         elif len(args) == 3:
             nx, ny, nz = (int(a) for a in args)
             self.voxelizedVolume_ = np.ones((ny, nx, nz), dtype=np.int32)
             self.eleSize_ = (1.0, 1.0, 1.0)
+            self.boundingBox_ = np.array([[0.0, 0.0, 0.0], [nx, ny, nz]], dtype=np.float64)
         else:
             raise GMGSError(L.ERR_INVALID_ARGUMENT, "Wrong input for voxelization!")
         self._solver = None
@@ -326,3 +329,41 @@ class Session:
     def GetCartesianStress(self):
         self.cartesianStressField_ = self._solver.stress(per_voxel=False)
         return self.cartesianStressField_
+
+    # ------------------------------------------------ output formats
+    def _grid(self):
+        """(resolution (x, y, z), padded occupancy, bounding box after padding)
+        as DiscretizeDesignDomain.m:37-63 leaves them."""
+        if self._solver is None:
+            self.DiscretizeDesignDomain()
+        ny, nx, nz = self._solver.padded_dims
+        vox = np.zeros((ny, nx, nz), dtype=np.int32)
+        oy, ox, oz = self.voxelizedVolume_.shape
+        vox[:oy, :ox, :oz] = self.voxelizedVolume_
+        bb = self.boundingBox_
+        if bb is None:
+            bb = np.array([[0.0, 0.0, 0.0], [ox * self.eleSize_[0], oy * self.eleSize_[1], oz * self.eleSize_[2]]])
+        bb = np.array(bb, dtype=np.float64)
+        bb[1] = bb[0] + (bb[1] - bb[0]) * np.array([nx, ny, nz], dtype=np.float64) / np.array([ox, oy, oz], dtype=np.float64)
+        return (nx, ny, nz), vox, bb
+
+    def ExportDataset_3DTSV(self, path="dataset_TSV.carti"):
+        """The .carti stress dataset (src/common/ExportDataset_3DTSV.m:1-42)."""
+        if self.cartesianStressField_ is None:
+            import warnings
+            warnings.warn("No Cartesian Stress Available!")
+            return None
+        from . import export
+        res, vox, bb = self._grid()
+        ele, nod = export.grid_maps(vox)
+        export.export_dataset_3dtsv(path, res, bb[0], bb[1], ele, nod, self.fixingCond_, self.loadingCond_,
+                                    self.cartesianStressField_)
+        return path
+
+    def WrapVoxelFEAmodel(self, path="wrappedVoxelFEAmodel.txt"):
+        """The wrapped voxel FEA model (src/common/WrapVoxelFEAmodel.m:1-26)."""
+        from . import export
+        res, vox, _ = self._grid()
+        ele, nod = export.grid_maps(vox)
+        export.wrap_voxel_fea_model(path, res, ele, nod, self.fixingCond_, self.loadingCond_)
+        return path

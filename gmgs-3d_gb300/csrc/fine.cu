@@ -90,6 +90,7 @@ struct EpiData {
     float q[3];       // FM_CG_UPDATE_JACOBI
     float pp[3];      // FM_CG_UPDATE_JACOBI: p
     double r64[3];    // FM_CG_UPDATE_JACOBI
+    double x64[3];    // FM_CG_UPDATE_JACOBI: loaded with the other operands, before the stencil
 };
 
 template <int MODE>
@@ -101,6 +102,7 @@ __device__ __forceinline__ void epi_fetch(const FineArgs& a, int S, int n, EpiDa
         if (MODE == FM_CG_UPDATE_JACOBI) {
             d.r[c] = a.r32[i];
             d.r64[c] = a.r64[i];
+            d.x64[c] = a.x64[i];
             if (!a.first) {
                 d.q[c] = a.q32[i];
                 d.pp[c] = a.pold[i];
@@ -221,7 +223,7 @@ __global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? 3 : 4)
                         rinc = fmaf(alpha, ed.q[b], rinc);
                         rm32 = fmaf(-alpha, ed.q[b], rm32);
                     }
-                    a.x64[i] += (double)xinc;
+                    a.x64[i] = ed.x64[b] + (double)xinc;
                     const double rn = ed.r64[b] - (double)rinc;
                     a.r64[i] = rn;
                     a.r32out[i] = (float)rn;

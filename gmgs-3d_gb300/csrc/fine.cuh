@@ -56,7 +56,6 @@ struct FineArgs {
     DotOut dot;
 };
 
-constexpr uint8_t NF_INTERIOR = 16;
 
 // displacement component a (0 = x, 1 = y, 2 = z) of stencil offset k = (dz+1)*9 + (dx+1)*3 + (dy+1)
 __host__ __device__ constexpr int off_y(int k) { return k % 3 - 1; }

@@ -99,6 +99,7 @@ __host__ __device__ constexpr int corner_of(int dy, int dx, int dz) {
 
 // node flag bits
 enum : uint8_t { NF_SOLID = 1, NF_FIX_X = 2, NF_FIX_Y = 4, NF_FIX_Z = 8 };
+constexpr uint8_t NF_INTERIOR = 16;  // all 8 surrounding elements carry the level's kscale * Ke0
 
 // ---------------------------------------------------------------------------
 // device-side views passed to kernels by value
@@ -212,14 +213,23 @@ struct Ctx {
 constexpr int KE = 576;
 
 // uniform element matrices in constant memory: [0] = Ke0 (FP64), [1] = Ke0 (FP32)
-void upload_ke0(const double* ke0_rowmajor);
+// Element matrix Ke0 (row = output DOF) and the assembled 27-point interior
+// stencil (3x3 block per offset k, offsets (k%3-1, k/3%3-1, k/9-1) in (y,x,z)),
+// passed to the operator kernels as a __grid_constant__ parameter so that
+// every handle carries its own material and voxel size.
+template <typename T>
+struct MatCoef {
+    T K[KE];
+    T S[243];
+};
+void make_mat_coef(const double* ke_rows, MatCoef<double>& c64, MatCoef<float>& c32);
 
 template <typename T> LevelView<T> view(const Level& L, double omega);
 
 // y = K_l x, fixed rows zeroed (AtX.m:1-58).  Tin/Tout let the mixed path read
 // FP64 CG vectors and compute in FP32.
 template <typename Tc, typename Tin, typename Tout>
-void launch_matvec(Ctx& c, const LevelView<Tc>& lv, const Tin* x, Tout* y, double kscale);
+void launch_matvec(Ctx& c, const LevelView<Tc>& lv, const MatCoef<Tc>& cf, const Tin* x, Tout* y, double kscale);
 
 // dx = (omega r) / d  (JacobiSmoother.m:5)
 template <typename Tr, typename Td, typename Tx>

@@ -666,7 +666,7 @@ void build_operators(Model& M) {
     for (int i = 0; i < 24; ++i)
         for (int j = 0; j < 24; ++j) KeT[i * 24 + j] = Ke[j * 24 + i];   // row = output DOF
     std::copy(KeT, KeT + KE, M.ke0_rows);
-    upload_ke0(KeT);
+    make_mat_coef(KeT, M.mc64, M.mc32);
     make_stencil(KeT, M.coef);
     for (int l = 0; l < L; ++l) {
         Level& lv = M.levels[l];

@@ -21,6 +21,8 @@ struct Model {
     double ke0_rows[KE];   // Ke0 with row = output DOF
     DevBuf ke0_dev;
     DevBuf galerkin_child; // 8 x 24x24: P_j^T Ke0 P_j per child position j
+    MatCoef<double> mc64;  // Ke0 and the interior stencil of this handle's material and voxel
+    MatCoef<float> mc32;
     DevBuf rho;            // compact density (double), extension
     // boundary conditions and solution (finest level, FP64, 3 planes)
     DevBuf F, U;
@@ -51,6 +53,10 @@ int64_t exclusive_scan(Ctx& c, int32_t* d, int64_t n);
 void element_stiffness(double E, double nu, const double ele[3], double Ke[KE]);
 // Isotropic Hooke coefficients (d11, d12, d44) and reciprocal element edges
 // (1/dx, 1/dy, 1/dz) for the stress kernels.
+template <typename T> inline const MatCoef<T>& mat_coef(const Model& M);
+template <> inline const MatCoef<double>& mat_coef<double>(const Model& M) { return M.mc64; }
+template <> inline const MatCoef<float>& mat_coef<float>(const Model& M) { return M.mc32; }
+
 void stress_coefficients(double E, double nu, const double ele[3], double c[6]);
 
 // setup.cu

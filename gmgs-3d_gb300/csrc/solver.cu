@@ -27,7 +27,7 @@ static void fine_matvec(Model& M, const Tin* x, Tout* y) {
     Level& l0 = M.levels[0];
     const double bytes = (double)l0.n_node * (3.0 * sizeof(Tin) + 3.0 * sizeof(Tout) + 1.0) + (double)l0.n_elem;
     M.ctx.mark(PK_FINE_MATVEC, false);
-    launch_matvec<Tc, Tin, Tout>(M.ctx, view<Tc>(l0, M.prm.omega), x, y, l0.kscale);
+    launch_matvec<Tc, Tin, Tout>(M.ctx, view<Tc>(l0, M.prm.omega), mat_coef<Tc>(M), x, y, l0.kscale);
     M.ctx.mark(PK_FINE_MATVEC, true, bytes);
 }
 
@@ -101,7 +101,7 @@ static void vcycle(Model& M, const T* r0, T* z) {
         const int64_t n3 = 3 * lv.g.slots;
         launch_jacobi_dx<T, T, T>(c, lv.g, v.diag, om, r, lv.vdx.as<T>());
         if (l == 0) fine_matvec<T, T, T>(M, lv.vdx.as<T>(), lv.vy.as<T>());
-        else launch_matvec<T, T, T>(c, v, lv.vdx.as<T>(), lv.vy.as<T>(), lv.kscale);
+        else launch_matvec<T, T, T>(c, v, mat_coef<T>(M), lv.vdx.as<T>(), lv.vy.as<T>(), lv.kscale);
         launch_diff<T>(c, n3, lv.vrp.as<T>(), r, lv.vy.as<T>());
         launch_restrict<T>(c, lv.g, lc.g, lc.nflag.as<uint8_t>(), lv.vrp.as<T>(), lc.vr.as<T>());
     }
@@ -137,7 +137,7 @@ void vcycle_apply_fp64(Model& M, const double* r, double* z) { vcycle_apply(M, r
 
 void apply_operator_dense(Model& M, int level, const double* x, double* y) {
     Level& lv = M.levels[level];
-    launch_matvec<double, double, double>(M.ctx, view<double>(lv, M.prm.omega), x, y, lv.kscale);
+    launch_matvec<double, double, double>(M.ctx, view<double>(lv, M.prm.omega), M.mc64, x, y, lv.kscale);
 }
 
 

@@ -50,3 +50,26 @@ def test_dot_dev(solver, n):
     assert v1 == v2                               # deterministic
     ref = float(np.dot(a, b))
     assert abs(v1 - ref) <= 1e-12 * np.sum(np.abs(a * b))
+
+
+def test_two_handles_with_different_materials_solve_independently():
+    """Element matrices and stencils are per handle (kernel parameters), so two
+    live handles with different voxel sizes and moduli do not interfere."""
+    import gmgs_oracle as G
+    from gmgs import Solver, synthetic
+    vox = synthetic.sphere_voids(12, 10, 16, 1, 21)
+    fixed, loads = synthetic.boundary_conditions(vox, 2)
+    cfg = [dict(ele_size=(1.0, 1.0, 1.0), youngs_modulus=1.0), dict(ele_size=(0.5, 1.5, 2.0), youngs_modulus=7.0)]
+    solvers, refs = [], []
+    for c in cfg:
+        s = Solver(vox, num_levels=2, omega=0.4, **c)
+        s.set_bc(fixed, loads)
+        solvers.append(s)
+        o = G.Oracle(vox, G.Params(num_levels=2, omega=0.4, youngs_modulus=c["youngs_modulus"]),
+                     ele_size=c["ele_size"])
+        o.apply_boundary_condition(fixed, loads)
+        refs.append(o.get_deformation())
+    for _ in range(2):                       # alternate: each solve must use its own handle's coefficients
+        for s, u_ref in zip(solvers, refs):
+            u = s.solve()
+            assert np.linalg.norm(u - u_ref) / np.linalg.norm(u_ref) < 1e-6

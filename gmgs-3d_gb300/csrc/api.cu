@@ -356,6 +356,9 @@ int gmgs_apply_operator(gmgs_handle* h, int32_t level, const double* x, double* 
         if (!h || !x || !y) fail(GMGS_ERR_INVALID_ARGUMENT, "NULL argument");
         gmgs::Model& M = h->M;
         if (level < 1 || level > M.num_levels) fail(GMGS_ERR_INVALID_ARGUMENT, "level out of range");
+        if (level == 2 && M.lean_level1)
+            fail(GMGS_ERR_STATE, "level 2 keeps only FP32 element matrices on a mixed-precision handle with a density "
+                                 "field; use an FP64 handle to apply it");
         ensure_coarse(h);
         gmgs::Level& lv = M.levels[level - 1];
         const int64_t nn = lv.n_node, S = lv.g.slots;
@@ -398,6 +401,9 @@ int gmgs_apply_operator_dev(gmgs_handle* h, int32_t level, const double* x, doub
         if (!h || !x || !y) fail(GMGS_ERR_INVALID_ARGUMENT, "NULL argument");
         gmgs::Model& M = h->M;
         if (level < 1 || level > M.num_levels) fail(GMGS_ERR_INVALID_ARGUMENT, "level out of range");
+        if (level == 2 && M.lean_level1)
+            fail(GMGS_ERR_STATE, "level 2 keeps only FP32 element matrices on a mixed-precision handle with a density "
+                                 "field; use an FP64 handle to apply it");
         ensure_coarse(h);
         gmgs::Level& lv = M.levels[level - 1];
         const int64_t nn = lv.n_node, S = lv.g.slots;

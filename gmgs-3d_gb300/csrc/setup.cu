@@ -369,7 +369,7 @@ __global__ void __launch_bounds__(192) k_galerkin(Grid gc, Grid gf, const int32_
                                                   const uint8_t* __restrict__ emf, const int32_t* __restrict__ etf,
                                                   const double* __restrict__ Ksf, const double* __restrict__ G,
                                                   double kscale_f, const double* __restrict__ escale_f,
-                                                  double* __restrict__ Ks_out) {
+                                                  double* __restrict__ Ks_out, float* __restrict__ Ks32_out) {
     __shared__ double K[KE], T[KE], W[64];
     const int64_t s = kslot[blockIdx.x];
     int Ey, Ex, Ez;
@@ -410,6 +410,36 @@ __global__ void __launch_bounds__(192) k_galerkin(Grid gc, Grid gf, const int32_
         }
         __syncthreads();
     }
+    for (int k = 0; k < 3; ++k) {
+        const int64_t o = (int64_t)blockIdx.x * KE + threadIdx.x + k * blockDim.x;
+        if (Ks_out) Ks_out[o] = acc[k];
+        if (Ks32_out) Ks32_out[o] = (float)acc[k];
+    }
+}
+
+// Level 3 straight from the finest level when every level-2 element is the
+// scaled-children sum sum_j s_j G_j (a density field): K = sum over the 64
+// finest descendants of s * G2[c][j], G2[c][j] = P_c^T G_j P_c, so the
+// level-2 matrices are never needed in FP64.  One block per coarse element.
+__global__ void __launch_bounds__(192) k_galerkin_grand(Grid g2, Grid g1, Grid g0, const int32_t* __restrict__ kslot,
+                                                        const uint8_t* __restrict__ em1, const uint8_t* __restrict__ em0,
+                                                        const double* __restrict__ esc0, double kscale0,
+                                                        const double* __restrict__ G2, double* __restrict__ Ks_out) {
+    const int64_t s = kslot[blockIdx.x];
+    int Ey, Ex, Ez;
+    slot_coords(g2, s, Ey, Ex, Ez);
+    double acc[3] = {0, 0, 0};
+    for (int c = 0; c < 8; ++c) {
+        const int cy = 2 * Ey + (c & 1), cx = 2 * Ex + ((c >> 1) & 1), cz = 2 * Ez + (c >> 2);
+        if (!em1[g1.slot(cy, cx, cz)]) continue;          // uniform branch across the block
+        for (int j = 0; j < 8; ++j) {
+            const int64_t fs = g0.slot(2 * cy + (j & 1), 2 * cx + ((j >> 1) & 1), 2 * cz + (j >> 2));
+            if (!em0[fs]) continue;
+            const double sc = kscale0 * esc0[fs];
+            const double* Gc = G2 + (int64_t)(c * 8 + j) * KE;
+            for (int k = 0; k < 3; ++k) acc[k] += sc * Gc[threadIdx.x + k * blockDim.x];
+        }
+    }
     for (int k = 0; k < 3; ++k) Ks_out[(int64_t)blockIdx.x * KE + threadIdx.x + k * blockDim.x] = acc[k];
 }
 
@@ -437,6 +467,42 @@ __global__ void k_diag(Grid g, const uint8_t* __restrict__ emask, const uint8_t*
         d[s] = a[0];
         d[s + g.slots] = a[1];
         d[s + 2 * g.slots] = a[2];
+    }
+}
+
+// Level-2 diagonal when its element matrices are the scaled-children sums
+// sum_j s_j G_j and only their FP32 copies are kept: each element's diagonal
+// entry is summed exactly as k_galerkin sums it, so the result equals k_diag
+// on the FP64 matrices.
+__global__ void k_diag_children(Grid g1, Grid g0, const uint8_t* __restrict__ em1, const uint8_t* __restrict__ nflag1,
+                                const uint8_t* __restrict__ em0, const double* __restrict__ esc0, double kscale0,
+                                const double* __restrict__ G, double* __restrict__ d) {
+    GRID_STRIDE(s, g1.slots) {
+        double a[3] = {0, 0, 0};
+        if (nflag1[s] & NF_SOLID) {
+            for (int e = 0; e < 8; ++e) {
+                const int A = e & 1, B = (e >> 1) & 1, C = e >> 2;
+                const int64_t es = s - A - B * g1.sx() - C * g1.sz();
+                if (!em1[es]) continue;
+                int Ey, Ex, Ez;
+                slot_coords(g1, es, Ey, Ex, Ez);
+                const int cn = corner_of(A, B, C);
+                for (int al = 0; al < 3; ++al) {
+                    const int ii = (3 * cn + al) * 24 + 3 * cn + al;
+                    double v = 0;
+                    for (int j = 0; j < 8; ++j) {
+                        const int64_t fs = g0.slot(2 * Ey + (j & 1), 2 * Ex + ((j >> 1) & 1), 2 * Ez + (j >> 2));
+                        if (!em0[fs]) continue;
+                        const double sc = kscale0 * esc0[fs];
+                        v += sc * G[j * KE + ii];
+                    }
+                    a[al] += v;
+                }
+            }
+        }
+        d[s] = a[0];
+        d[s + g1.slots] = a[1];
+        d[s + 2 * g1.slots] = a[2];
     }
 }
 
@@ -695,8 +761,7 @@ void build_operators(Model& M) {
     const double* ke0 = M.ke0_dev.as<double>();
     // G_j = P_j^T Ke0 P_j for the 8 child positions j (SetupSolver.m:53-66 applied to one solid child)
     static_assert(KE == 576, "24x24 element matrices");
-    std::vector<double> Gh(8 * KE, 0.0);
-    for (int j = 0; j < 8; ++j) {
+    auto child_product = [](const double* K, int j, double* out) {     // out = P_j^T K P_j
         const int dy = j & 1, dx = (j >> 1) & 1, dz = j >> 2;
         double W[8][8];
         for (int q = 0; q < 8; ++q)
@@ -709,29 +774,60 @@ void build_operators(Model& M) {
         for (int r = 0; r < 24; ++r)
             for (int col = 0; col < 24; ++col) {
                 double v = 0;
-                for (int q = 0; q < 8; ++q) v += KeT[r * 24 + 3 * q + col % 3] * W[q][col / 3];
+                for (int q = 0; q < 8; ++q) v += K[r * 24 + 3 * q + col % 3] * W[q][col / 3];
                 T[r * 24 + col] = v;
             }
         for (int row = 0; row < 24; ++row)
             for (int col = 0; col < 24; ++col) {
                 double v = 0;
                 for (int p = 0; p < 8; ++p) v += W[p][row / 3] * T[(3 * p + row % 3) * 24 + col];
-                Gh[j * KE + row * 24 + col] = v;
+                out[row * 24 + col] = v;
             }
-    }
+    };
+    std::vector<double> Gh(8 * KE, 0.0);
+    for (int j = 0; j < 8; ++j) child_product(KeT, j, &Gh[j * KE]);
     M.galerkin_child = dalloc(8 * KE * sizeof(double));
     GMGS_CUDA(cudaMemcpyAsync(M.galerkin_child.p, Gh.data(), 8 * KE * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    // Mixed precision with a density field: the level-2 matrices are kept in
+    // FP32 only and level 3 is built from the 64 finest descendants
+    // (about 60 % less device memory on large models).
+    const bool lean = M.has_density && M.prm.precision == GMGS_MIXED && L >= 3;
+    DevBuf G2;
+    if (lean) {
+        std::vector<double> G2h(64 * KE);
+        for (int cc = 0; cc < 8; ++cc)
+            for (int j = 0; j < 8; ++j) child_product(&Gh[j * KE], cc, &G2h[(cc * 8 + j) * KE]);
+        G2 = dalloc(64 * KE * sizeof(double));
+        GMGS_CUDA(cudaMemcpyAsync(G2.p, G2h.data(), 64 * KE * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    }
+    M.lean_level1 = lean;
     // Galerkin matrices level by level
     for (int l = 1; l < L; ++l) {
         Level& lv = M.levels[l];
         Level& fv = M.levels[l - 1];
+        if (lean && l == 1) {
+            lv.Ks64.release();
+            lv.Ks32 = dalloc(std::max<int64_t>(1, lv.nK) * KE * sizeof(float));
+            if (lv.nK > 0) {
+                k_galerkin<<<(unsigned)lv.nK, 192, 0, c.stream>>>(
+                    lv.g, fv.g, lv.kslot.as<int32_t>(), fv.emask.as<uint8_t>(), fv.etype.as<int32_t>(), nullptr,
+                    M.galerkin_child.as<double>(), fv.kscale, fv.escale64.as<double>(), nullptr, lv.Ks32.as<float>());
+                GMGS_LAUNCHED(c);
+            }
+            continue;
+        }
         lv.Ks64 = dalloc(std::max<int64_t>(1, lv.nK) * KE * sizeof(double));
-        if (lv.nK > 0) {
+        if (lv.nK > 0 && lean && l == 2) {
+            Level& l0 = M.levels[0];
+            k_galerkin_grand<<<(unsigned)lv.nK, 192, 0, c.stream>>>(
+                lv.g, fv.g, l0.g, lv.kslot.as<int32_t>(), fv.emask.as<uint8_t>(), l0.emask.as<uint8_t>(),
+                l0.escale64.as<double>(), l0.kscale, G2.as<double>(), lv.Ks64.as<double>());
+            GMGS_LAUNCHED(c);
+        } else if (lv.nK > 0) {
             k_galerkin<<<(unsigned)lv.nK, 192, 0, c.stream>>>(
                 lv.g, fv.g, lv.kslot.as<int32_t>(), fv.emask.as<uint8_t>(), fv.etype.as<int32_t>(),
                 fv.Ks64.as<double>(), M.galerkin_child.as<double>(), fv.kscale,
-                l == 1 ? fv.escale64.as<double>() : nullptr,
-                lv.Ks64.as<double>());
+                l == 1 ? fv.escale64.as<double>() : nullptr, lv.Ks64.as<double>(), nullptr);
             GMGS_LAUNCHED(c);
         }
     }
@@ -740,13 +836,20 @@ void build_operators(Model& M) {
         Level& lv = M.levels[l];
         if (l < L - 1) {
             lv.diag64 = dalloc(3 * lv.g.slots * sizeof(double));
-            k_diag<<<blocks_for(c, lv.g.slots), 256, 0, c.stream>>>(
-                lv.g, lv.emask.as<uint8_t>(), lv.nflag.as<uint8_t>(), lv.etype.as<int32_t>(), lv.Ks64.as<double>(),
-                ke0, lv.kscale, l == 0 ? lv.escale64.as<double>() : nullptr, lv.diag64.as<double>());
+            if (lean && l == 1) {
+                Level& l0 = M.levels[0];
+                k_diag_children<<<blocks_for(c, lv.g.slots), 256, 0, c.stream>>>(
+                    lv.g, l0.g, lv.emask.as<uint8_t>(), lv.nflag.as<uint8_t>(), l0.emask.as<uint8_t>(),
+                    l0.escale64.as<double>(), l0.kscale, M.galerkin_child.as<double>(), lv.diag64.as<double>());
+            } else {
+                k_diag<<<blocks_for(c, lv.g.slots), 256, 0, c.stream>>>(
+                    lv.g, lv.emask.as<uint8_t>(), lv.nflag.as<uint8_t>(), lv.etype.as<int32_t>(), lv.Ks64.as<double>(),
+                    ke0, lv.kscale, l == 0 ? lv.escale64.as<double>() : nullptr, lv.diag64.as<double>());
+            }
             GMGS_LAUNCHED(c);
         }
         if (M.prm.precision == GMGS_MIXED) {
-            if (lv.nK > 0 && l < L - 1) {
+            if (lv.nK > 0 && l < L - 1 && !(lean && l == 1)) {
                 lv.Ks32 = dalloc(lv.nK * KE * sizeof(float));
                 k_to_float<<<blocks_for(c, lv.nK * KE), 256, 0, c.stream>>>(lv.nK * KE, lv.Ks64.as<double>(),
                                                                              lv.Ks32.as<float>());

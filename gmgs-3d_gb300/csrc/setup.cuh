@@ -21,6 +21,7 @@ struct Model {
     double ke0_rows[KE];   // Ke0 with row = output DOF
     DevBuf ke0_dev;
     DevBuf galerkin_child; // 8 x 24x24: P_j^T Ke0 P_j per child position j
+    bool lean_level1 = false; // level-2 (index 1) matrices kept in FP32 only (mixed precision + density)
     MatCoef<double> mc64;  // Ke0 and the interior stencil of this handle's material and voxel
     MatCoef<float> mc32;
     DevBuf rho;            // compact density (double), extension

@@ -165,3 +165,32 @@ def test_block84_adjoint_central_differences_64_voxels():
             worst = max(worst, err)
             assert err <= 1e-4, (int(e), fd, g[e])
     print(f"worst relative FD error {worst:.2e}")
+
+
+def test_mixed_density_three_levels_fp32_only_level2():
+    """Mixed precision with a density field keeps the level-2 Galerkin matrices
+    in FP32 only and builds level 3 from the 64 finest descendants; the solve
+    and the gradient still match the FP64 path, and the FP64 operator of
+    level 2 is reported as unavailable."""
+    from gmgs.solver import GMGSError
+    import gmgs._lib as L
+    vox = synthetic.sphere_voids(24, 20, 28, 3, 17)
+    fixed, loads = synthetic.boundary_conditions(vox, 3)
+    rho = synthetic.density(int(vox.sum()), (0.3, 1.0), 17)
+    out = {}
+    for prec in ("fp64", "mixed"):
+        s = Solver(vox, num_levels=3, omega=0.4, tol=1e-6, max_it=2000, precision=prec)
+        s.set_bc(fixed, loads)
+        s.set_density(rho, 3.0)
+        u = s.solve()
+        assert s.status == 0
+        out[prec] = (u, s.iterations, s.grad(), s)
+    (u64, it64, g64, s64), (u32, it32, g32, s32) = out["fp64"], out["mixed"]
+    assert abs(it32 - it64) <= 1
+    assert np.linalg.norm(u32 - u64) / np.linalg.norm(u64) < 1e-5
+    assert np.linalg.norm(g32 - g64) / np.linalg.norm(g64) < 1e-4
+    x = np.random.default_rng(0).standard_normal(3 * s64.num_nodes(2))
+    s64.apply_operator(x, level=2)                     # FP64 handle: available
+    with pytest.raises(GMGSError) as e:
+        s32.apply_operator(x, level=2)
+    assert e.value.status == L.ERR_STATE

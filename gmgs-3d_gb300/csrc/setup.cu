@@ -6,7 +6,7 @@
 // src/kernel/BuildingMeshHierarchy.m:8-142, src/kernel/SetupSolver.m:9-259,
 // src/kernel/DirectlyAssembleStifnessMatrix.m:24-34,
 // src/common/ApplyBoundaryCondition.m:7-23.
-#include <cublas_api.h>
+#include <cublas_v2.h>
 #include <cusolverDn.h>
 
 #include <algorithm>
@@ -614,6 +614,20 @@ __global__ void k_symmetrize_lower(int n, double* A) {
     }
 }
 
+// half bandwidth of the assembled coarsest matrix: max (col - row) over
+// non-zeros; one warp per row, coalesced
+__global__ void k_bandwidth(int n, const double* __restrict__ A, int* __restrict__ bw) {
+    const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= n) return;
+    const double* row = A + w * (int64_t)n;
+    int last = (int)w;
+    for (int c = (int)w + lane; c < n; c += 32)
+        if (row[c] != 0.0) last = c;
+    for (int o = 16; o > 0; o >>= 1) last = max(last, __shfl_xor_sync(0xffffffffu, last, o));
+    if (lane == 0) atomicMax(bw, last - (int)w);
+}
+
 __global__ void k_to_float(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
     GRID_STRIDE(i, n) b[i] = (float)a[i];
 }
@@ -976,30 +990,94 @@ void build_coarse_bc(Model& M) {
     if (cusolverDnCreate(&hs) != CUSOLVER_STATUS_SUCCESS) throw Error(GMGS_ERR_CUDA, "cusolverDnCreate failed");
     struct Guard { cusolverDnHandle_t h; ~Guard() { cusolverDnDestroy(h); } } guard{hs};
     cusolverDnSetStream(hs, c.stream);
+    const int n = (int)nf;
+    double* A = M.kinv.as<double>();
+    // The free DOFs are numbered node by node in slot order, so K is banded:
+    // with blocks at least as wide as the half bandwidth it is block
+    // tridiagonal, its Cholesky factor block bidiagonal (block potrf / trsm /
+    // syrk), and the inverse factor follows block row by block row from
+    //   Linv_ii = L_ii^-1,  Linv_ij = -Linv_ii C_i Linv_(i-1)j  (j < i),
+    // C_i the sub-diagonal block of L: about a quarter of the flops of dense
+    // potrf + trtri, with the same result in the same place.
+    int bw = 0;
+    {
+        DevBuf dbw = dalloc(sizeof(int));
+        GMGS_CUDA(cudaMemsetAsync(dbw.p, 0, sizeof(int), c.stream));
+        k_bandwidth<<<(unsigned)(((int64_t)n * 32 + 255) / 256), 256, 0, c.stream>>>(n, A, dbw.as<int>());
+        GMGS_LAUNCHED(c);
+        GMGS_CUDA(cudaMemcpyAsync(&bw, dbw.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+        GMGS_CUDA(cudaStreamSynchronize(c.stream));
+    }
+    const int B = std::max(32, (bw + 31) / 32 * 32);
+    const int nb = (n + B - 1) / B;
+    auto bsz = [&](int i) { return std::min(B, n - i * B); };
+    const int fmax = nb >= 3 ? B : n;                 // largest potrf / trtri order
     int lwork = 0;
     size_t tw_dev = 0, tw_host = 0;
-    const int n = (int)nf;
-    if (cusolverDnDpotrf_bufferSize(hs, CUBLAS_FILL_MODE_LOWER, n, M.kinv.as<double>(), n, &lwork) !=
-            CUSOLVER_STATUS_SUCCESS ||
-        cusolverDnXtrtri_bufferSize(hs, CUBLAS_FILL_MODE_LOWER, CUBLAS_DIAG_NON_UNIT, n, CUDA_R_64F, M.kinv.p, n,
-                                    &tw_dev, &tw_host) != CUSOLVER_STATUS_SUCCESS)
+    if (cusolverDnDpotrf_bufferSize(hs, CUBLAS_FILL_MODE_LOWER, fmax, A, n, &lwork) != CUSOLVER_STATUS_SUCCESS ||
+        cusolverDnXtrtri_bufferSize(hs, CUBLAS_FILL_MODE_LOWER, CUBLAS_DIAG_NON_UNIT, fmax, CUDA_R_64F, A, n, &tw_dev,
+                                    &tw_host) != CUSOLVER_STATUS_SUCCESS)
         throw Error(GMGS_ERR_CUDA, "cuSOLVER buffer size query failed");
     DevBuf work = dalloc(std::max((size_t)lwork * sizeof(double), tw_dev));
     std::vector<unsigned char> hwork(std::max<size_t>(1, tw_host));
-    DevBuf info = dalloc(sizeof(int));
-    if (cusolverDnDpotrf(hs, CUBLAS_FILL_MODE_LOWER, n, M.kinv.as<double>(), n, work.as<double>(), lwork,
-                         info.as<int>()) != CUSOLVER_STATUS_SUCCESS)
-        throw Error(GMGS_ERR_CUDA, "cusolverDnDpotrf failed");
-    int hinfo = 0;
-    GMGS_CUDA(cudaMemcpyAsync(&hinfo, info.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    DevBuf info = dalloc(2 * sizeof(int) * std::max(1, nb));
+    GMGS_CUDA(cudaMemsetAsync(info.p, 0, 2 * sizeof(int) * std::max(1, nb), c.stream));
+    auto potrf = [&](int m, double* a, int* inf) {
+        if (cusolverDnDpotrf(hs, CUBLAS_FILL_MODE_LOWER, m, a, n, work.as<double>(), lwork, inf) != CUSOLVER_STATUS_SUCCESS)
+            throw Error(GMGS_ERR_CUDA, "cusolverDnDpotrf failed");
+    };
+    auto trtri = [&](int m, double* a, int* inf) {
+        if (cusolverDnXtrtri(hs, CUBLAS_FILL_MODE_LOWER, CUBLAS_DIAG_NON_UNIT, m, CUDA_R_64F, a, n, work.p, tw_dev,
+                             hwork.data(), tw_host, inf) != CUSOLVER_STATUS_SUCCESS)
+            throw Error(GMGS_ERR_CUDA, "cusolverDnXtrtri failed");
+    };
+    int* infos = info.as<int>();
+    if (nb < 3) {
+        potrf(n, A, infos);
+        trtri(n, A, infos + 1);
+    } else {
+        cublasHandle_t hb = nullptr;
+        if (cublasCreate(&hb) != CUBLAS_STATUS_SUCCESS) throw Error(GMGS_ERR_CUDA, "cublasCreate failed");
+        struct BGuard { cublasHandle_t h; ~BGuard() { cublasDestroy(h); } } bguard{hb};
+        cublasSetStream(hb, c.stream);
+        auto ok = [](cublasStatus_t st, const char* what) {
+            if (st != CUBLAS_STATUS_SUCCESS) throw Error(GMGS_ERR_CUDA, std::string(what) + " failed");
+        };
+        const double one = 1.0, mone = -1.0, zero = 0.0;
+        auto blk = [&](int bi, int bj) { return A + (int64_t)bi * B + (int64_t)bj * B * n; };   // column-major block
+        for (int i = 0; i < nb; ++i) {                  // block Cholesky, column-major lower
+            potrf(bsz(i), blk(i, i), infos + 2 * i);
+            if (i + 1 < nb) {
+                ok(cublasDtrsm(hb, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT,
+                               bsz(i + 1), bsz(i), &one, blk(i, i), n, blk(i + 1, i), n), "cublasDtrsm");
+                ok(cublasDsyrk(hb, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, bsz(i + 1), bsz(i), &mone, blk(i + 1, i), n,
+                               &one, blk(i + 1, i + 1), n), "cublasDsyrk");
+            }
+        }
+        for (int i = 0; i < nb; ++i) trtri(bsz(i), blk(i, i), infos + 2 * i + 1);
+        DevBuf T = dalloc((size_t)B * n * sizeof(double));
+        double* t = T.as<double>();
+        for (int i = 1; i < nb; ++i) {                  // block row i of Linv
+            const int bi = bsz(i), bp = bsz(i - 1), w0 = (i - 1) * B;
+            if (w0 > 0)                                 // T[:, 0:w0] = C_i Linv[i-1, 0:w0]
+                ok(cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, bi, w0, bp, &one, blk(i, i - 1), n, blk(i - 1, 0), n,
+                               &zero, t, bi), "cublasDgemm");
+            // T[:, w0:w0+bp] = C_i Linv[i-1, i-1] (lower triangular)
+            ok(cublasDtrmm(hb, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, bi, bp,
+                           &one, blk(i - 1, i - 1), n, blk(i, i - 1), n, t + (int64_t)w0 * bi, bi), "cublasDtrmm");
+            // Linv[i, 0:w0+bp] = -Linv_ii T
+            ok(cublasDtrmm(hb, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, bi,
+                           w0 + bp, &mone, blk(i, i), n, t, bi, blk(i, 0), n), "cublasDtrmm");
+        }
+        GMGS_CUDA(cudaStreamSynchronize(c.stream));
+    }
+    std::vector<int> hinfo(2 * std::max(1, nb));
+    GMGS_CUDA(cudaMemcpyAsync(hinfo.data(), info.p, hinfo.size() * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
     GMGS_CUDA(cudaStreamSynchronize(c.stream));
-    if (hinfo != 0) throw Error(GMGS_ERR_NOT_SPD, "coarsest-level matrix is not positive definite");
-    if (cusolverDnXtrtri(hs, CUBLAS_FILL_MODE_LOWER, CUBLAS_DIAG_NON_UNIT, n, CUDA_R_64F, M.kinv.p, n, work.p, tw_dev,
-                         hwork.data(), tw_host, info.as<int>()) != CUSOLVER_STATUS_SUCCESS)
-        throw Error(GMGS_ERR_CUDA, "cusolverDnXtrtri failed");
-    GMGS_CUDA(cudaMemcpyAsync(&hinfo, info.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
-    GMGS_CUDA(cudaStreamSynchronize(c.stream));
-    if (hinfo != 0) throw Error(GMGS_ERR_NOT_SPD, "coarsest-level factor is singular");
+    for (size_t k = 0; k < hinfo.size(); k += 2)
+        if (hinfo[k] != 0) throw Error(GMGS_ERR_NOT_SPD, "coarsest-level matrix is not positive definite");
+    for (size_t k = 1; k < hinfo.size(); k += 2)
+        if (hinfo[k] != 0) throw Error(GMGS_ERR_NOT_SPD, "coarsest-level factor is singular");
     k_symmetrize_lower<<<blocks_for(c, (int64_t)n * n), 256, 0, c.stream>>>(n, M.kinv.as<double>());
     GMGS_LAUNCHED(c);
     M.cvec_tmp = dalloc(nf * sizeof(double));

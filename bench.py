@@ -342,13 +342,18 @@ def run_gmgs(a):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             se = Solver(vox, omega=a.omega, num_levels=L, tol=w.tol, precision="mixed")
+            t1 = time.perf_counter()
             se.set_bc(fixed, loads)
             if rho is not None:
                 se.set_density(rho, 3.0)
+            t2 = time.perf_counter()
             u = se.solve()
             torch.cuda.synchronize()
-            times.append(time.perf_counter() - t0)
+            t3 = time.perf_counter()
+            times.append(t3 - t0)
             phases = se.phase_times_ms
+            phases.update({"call_create_ms": (t1 - t0) * 1e3, "call_set_bc_ms": (t2 - t1) * 1e3,
+                           "call_solve_ms": (t3 - t2) * 1e3})
             se.close()
         e2e = {"value": times[-1], "unit": "s", "h2d_bytes_per_step": int(occ_bytes + bc_bytes),
                "d2h_bytes_per_step": int(u.nbytes), "phases_ms": phases}

@@ -156,7 +156,8 @@ def make(workload: Workload | str, scale: float = 1.0):
     rho = None
     if w.rho_range is not None:
         rho = density(int(vox.sum()), w.rho_range, w.seed)
-    return vox, fixed, loads, L, rho
+    # the reference's voxelizedVolume_ is a column-major (y, x, z) array
+    return np.asfortranarray(vox), fixed, loads, L, rho
 
 
 # ---------------------------------------------------------------------------

@@ -169,6 +169,17 @@ def cpu_extrapolate(sample: dict, dofs_full: int, its_full: int) -> float:
 
 
 # --------------------------------------------------------------------------
+def max_over_ranks(value: float, device: str = "cpu") -> float:
+    """The slowest rank's value (the job finishes when its last replica does)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return value
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -272,9 +283,7 @@ def run_gmgs(a):
                            "ms_per_launch": ms_k / max(n_k, 1),
                            "gbs": (b_k / (ms_k / 1e3) / 1e9) if (b_k and ms_k) else None}
     if ws > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = max_over_ranks(ms, "cuda")
 
     out = {}
     if rank == 0:

@@ -124,6 +124,14 @@ __global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? 3 : 4)
     const int y0 = blockIdx.x * TY, x0 = blockIdx.y * TX;
     const int zb = blockIdx.z * zc;
     const int ze = min(zb + zc, g.nz + 1);        // node planes [zb, ze)
+    if (L.tile_occ) {                             // no solid node in this column tile: nothing to compute
+        int any = 0;
+        for (int iz = zb; iz < ze; ++iz) any |= L.tile_occ[((int64_t)iz * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x];
+        if (!any) {
+            if (MODE == FM_CG_DIRECTION || MODE == FM_CG_UPDATE_JACOBI) grid_dot_finish(0.0, a.dot, sh);
+            return;
+        }
+    }
     // warps cover 8 (y) x 4 (x) node patches, so a face of the domain
     // crosses few warps and the boundary path rarely diverges
     const int tid = threadIdx.x + threadIdx.y * TY;
@@ -414,6 +422,26 @@ void launch_perel_vdown(Ctx& c, const FineLevel& L, const Coef32& cf, const int3
     if (count <= 0) return;
     const int blocks = (int)(((int64_t)count * 32 + 255) / 256);
     k_perel_vdown<<<blocks, 256, 0, c.stream>>>(L, cf, nodes, count, r, w, out);
+    GMGS_LAUNCHED(c);
+}
+
+// occupancy of the streaming kernel's node tiles: one block per (y tile,
+// x tile, z plane), 1 when any of its 32 x 8 nodes is solid.  Real geometry
+// leaves most of the padded box empty; CTAs whose whole z-chunk of tiles is
+// empty skip all work.
+__global__ void k_tile_occ(Grid g, const uint8_t* __restrict__ nflag, uint8_t* __restrict__ occ) {
+    const int ty = threadIdx.x & 31, tx = threadIdx.x >> 5;
+    const int iy = blockIdx.x * TY + ty, ix = blockIdx.y * TX + tx, iz = blockIdx.z;
+    const bool solid = iy <= g.ny && ix <= g.nx && (nflag[g.slot(iy, ix, iz)] & NF_SOLID);
+    const int any = __syncthreads_or(solid);
+    if (threadIdx.x == 0) occ[((int64_t)iz * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = any ? 1 : 0;
+}
+size_t tile_occ_bytes(const Grid& g) {
+    return (size_t)((g.ny + 1 + TY - 1) / TY) * ((g.nx + 1 + TX - 1) / TX) * (g.nz + 1);
+}
+void launch_tile_occ(Ctx& c, const Grid& g, const uint8_t* nflag, uint8_t* occ) {
+    dim3 grid((g.ny + 1 + TY - 1) / TY, (g.nx + 1 + TX - 1) / TX, g.nz + 1);
+    k_tile_occ<<<grid, NT, 0, c.stream>>>(g, nflag, occ);
     GMGS_LAUNCHED(c);
 }
 

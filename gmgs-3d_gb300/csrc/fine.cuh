@@ -22,6 +22,7 @@ struct FineLevel {
     const float* Ks;         // per-element matrices (FP32), row = output DOF
     const float* escale;     // finest-level element scale or null
     float kscale;
+    const uint8_t* tile_occ; // per (z plane, x tile, y tile) of the streaming kernel: any solid node; null = all
 };
 
 struct DotOut {
@@ -235,6 +236,8 @@ void launch_wdinv(Ctx& c, int64_t n, const double* d, double omega, float* w);
 void launch_perel_vdown(Ctx& c, const FineLevel& L, const Coef32& cf, const int32_t* nodes, int count, const float* r,
                         const float* w, float* out);
 void launch_emask8(Ctx& c, const Grid& g, const uint8_t* emask, uint8_t* e8);
+size_t tile_occ_bytes(const Grid& g);
+void launch_tile_occ(Ctx& c, const Grid& g, const uint8_t* nflag, uint8_t* occ);
 void launch_to_f32(Ctx& c, int64_t n, const double* a, float* b);
 void launch_drop_last_dx(Ctx& c, int64_t n, double* x, const float* r32, const float* q, const float* w,
                          const double* scal, int cur, int first);

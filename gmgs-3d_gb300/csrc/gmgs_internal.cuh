@@ -162,6 +162,7 @@ struct Level {
     DevBuf elem_slot;         // compact element id -> slot (int32), eleMapBack order
     // V-cycle work vectors (3 planes each), precision of the V-cycle
     DevBuf vr, vrp, vdx, vx, vy;
+    DevBuf tile_occ;          // mixed path: per 32x8 node tile and z plane, 1 if it holds a solid node
     DevBuf wdinv32;           // mixed path: omega / diag in FP32
     DevBuf emask8;            // mixed path: per-node mask of the 8 surrounding solid elements
     DevBuf perel_nodes;       // slots of nodes touching an element with its own stored matrix

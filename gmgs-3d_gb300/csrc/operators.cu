@@ -147,6 +147,41 @@ __device__ __forceinline__ void interior_pairs(const MatCoef<Tc>& cf, const Tin*
     a0 = acc[0]; a1 = acc[1]; a2 = acc[2];
 }
 
+// the void-element complement applies when the level has no per-element
+// scale, every solid element around the node carries the uniform matrix and
+// at least four of the eight are solid
+template <typename Tc>
+__device__ __forceinline__ bool complement_ok(const LevelView<Tc>& lv, int64_t n, int64_t sx, int64_t sz) {
+    if (lv.escale) return false;
+    int solid = 0;
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+        const int64_t es = n - (e & 1) - ((e >> 1) & 1) * sx - (e >> 2) * sz;
+        if (lv.emask[es]) {
+            ++solid;
+            if (lv.etype && lv.etype[es] > 0) return false;
+        }
+    }
+    return solid >= 4;
+}
+
+// rows of corner c of the uniform element at es, times s (run-time corner)
+template <typename Tc, typename Tin>
+__device__ __noinline__ void elem_rows_rt(const MatCoef<Tc>& cf, const Tin* __restrict__ x, int64_t es, int64_t S,
+                                          int64_t sx, int64_t sz, int c, Tc s, Tc& a0, Tc& a1, Tc& a2) {
+    Tc b0 = 0, b1 = 0, b2 = 0;
+#pragma unroll 1
+    for (int j = 0; j < 8; ++j) {
+        const int64_t ns = es + corner_y(j) + corner_x(j) * sx + corner_z(j) * sz;
+        const Tc x0 = (Tc)x[ns], x1 = (Tc)x[ns + S], x2 = (Tc)x[ns + 2 * S];
+        const Tc* k = cf.K + (3 * c) * 24 + 3 * j;
+        b0 += k[0] * x0 + k[1] * x1 + k[2] * x2;
+        b1 += k[24] * x0 + k[25] * x1 + k[26] * x2;
+        b2 += k[48] * x0 + k[49] * x1 + k[50] * x2;
+    }
+    a0 += s * b0; a1 += s * b1; a2 += s * b2;
+}
+
 template <typename Tc, typename Tin, typename Tout>
 __global__ void __launch_bounds__(128) k_matvec(LevelView<Tc> lv, const __grid_constant__ MatCoef<Tc> cf, Tc kscale,
                                                 const Tin* __restrict__ x, Tout* __restrict__ y) {
@@ -162,6 +197,19 @@ __global__ void __launch_bounds__(128) k_matvec(LevelView<Tc> lv, const __grid_c
     if (f & NF_INTERIOR) {
         interior_pairs<Tc, Tin>(cf, x, n, S, sx, sz, a0, a1, a2);
         a0 *= kscale; a1 *= kscale; a2 *= kscale;
+    } else if ((f & NF_SOLID) && complement_ok(lv, n, sx, sz)) {
+        // all solid elements uniform, at most four void: the assembled stencil
+        // minus the void elements' rows costs fewer operations than the solid
+        // elements' rows (AtX.m:34-56 sums the latter)
+        interior_pairs<Tc, Tin>(cf, x, n, S, sx, sz, a0, a1, a2);
+        a0 *= kscale; a1 *= kscale; a2 *= kscale;
+#pragma unroll 1
+        for (int e = 0; e < 8; ++e) {
+            const int A = e & 1, B = (e >> 1) & 1, Cz = e >> 2;
+            const int64_t es = n - A - B * sx - Cz * sz;
+            if (lv.emask[es]) continue;
+            elem_rows_rt<Tc, Tin>(cf, x, es, S, sx, sz, corner_of(A, B, Cz), -kscale, a0, a1, a2);
+        }
     } else if (f & NF_SOLID) {
         elem_contrib<Tc, Tin, 0>(lv, cf, kscale, x, n, S, sx, sz, a0, a1, a2);
         elem_contrib<Tc, Tin, 1>(lv, cf, kscale, x, n, S, sx, sz, a0, a1, a2);

@@ -51,6 +51,8 @@ void alloc_work(Model& M) {
                 launch_wdinv(c, (int64_t)n3, lv.diag64.as<double>(), M.prm.omega, lv.wdinv32.as<float>());
                 if (lv.emask8.bytes < (size_t)lv.g.slots) lv.emask8 = dalloc(lv.g.slots);
                 launch_emask8(c, lv.g, lv.emask.as<uint8_t>(), lv.emask8.as<uint8_t>());
+                if (lv.tile_occ.bytes < tile_occ_bytes(lv.g)) lv.tile_occ = dalloc(tile_occ_bytes(lv.g));
+                launch_tile_occ(c, lv.g, lv.nflag.as<uint8_t>(), lv.tile_occ.as<uint8_t>());
             }
         }
     }
@@ -154,6 +156,7 @@ static FineLevel fine_level(const Level& lv) {
     f.Ks = lv.Ks32.as<float>();
     f.escale = lv.escale32.as<float>();
     f.kscale = (float)lv.kscale;
+    f.tile_occ = lv.tile_occ.as<uint8_t>();
     return f;
 }
 

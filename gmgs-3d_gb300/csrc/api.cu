@@ -2,10 +2,16 @@
 // host <-> device copies and the call order of the reference's
 // GetDeformation() / GetCartesianStress() (src/kernel/GetDeformation.m:1-22,
 // src/kernel/GetCartesianStress.m:1-42).
+#include <unistd.h>
+
+#include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
+#include <thread>
+#include <vector>
 
 #include "setup.cuh"
 
@@ -45,6 +51,45 @@ int guarded(gmgs_handle* h, F&& f) {
 
 void fail(int status, const char* msg) { throw gmgs::Error(status, msg); }
 
+// A freshly allocated host output buffer is backed by pages the OS maps and
+// zeroes on first write; a device-to-host copy into such a buffer runs at the
+// page-fault rate of one core (about 20-25 GB/s for GB-sized outputs on the
+// Grace host) instead of the link rate (about 190 GB/s).  HostPrefault writes
+// one byte per page of the output from a few host threads while the GPU is
+// still computing, so the copy that follows finds every page mapped.  The
+// buffer is an output: its contents are overwritten by the copy anyway.
+class HostPrefault {
+public:
+    HostPrefault(void* p, size_t bytes) {
+        if (!p || bytes < kMinBytes) return;
+        const long pg = sysconf(_SC_PAGESIZE);
+        const size_t page = pg > 0 ? (size_t)pg : 4096;
+        const unsigned hc = std::thread::hardware_concurrency();
+        const size_t nt = std::min<size_t>(kMaxThreads, std::max<size_t>(1, hc / 2));
+        char* base = static_cast<char*>(p);
+        const size_t per = (bytes + nt - 1) / nt;
+        for (size_t t = 0; t < nt; ++t) {
+            const size_t b = t * per, e = std::min(bytes, b + per);
+            if (b >= e) break;
+            threads_.emplace_back([base, b, e, page]() {
+                volatile char* q = base;
+                for (size_t i = b; i < e; i += page) q[i] = 0;
+                q[e - 1] = 0;
+            });
+        }
+    }
+    void join() {
+        for (auto& t : threads_) t.join();
+        threads_.clear();
+    }
+    ~HostPrefault() { join(); }
+
+private:
+    static constexpr size_t kMinBytes = 32u << 20;
+    static constexpr size_t kMaxThreads = 8;
+    std::vector<std::thread> threads_;
+};
+
 // the reference's level rule (DiscretizeDesignDomain.m:29-41); returns numLevels
 int level_rule(int nely, int nelx, int nelz, const gmgs_params& p) {
     if (p.num_levels) {
@@ -69,8 +114,10 @@ void ensure_coarse(gmgs_handle* h) {
     if (!M.bc_set) fail(GMGS_ERR_STATE, "boundary conditions are not set");
     if (!M.coarse_ready) {
         const auto t0 = Clock::now();
+        M.ctx.trace_point("bc: start");
         gmgs::build_coarse_bc(M);
         gmgs::alloc_work(M);
+        M.ctx.trace_point("bc: work buffers");
         M.coarse_ready = true;
         M.t_bc_ms = ms_since(t0);
     }
@@ -97,7 +144,10 @@ int solve_impl(gmgs_handle* h, double* U_host, double* U_dev, int32_t* iters, do
     const size_t n3 = 3 * (size_t)l0.g.slots;
     if (M.U.bytes < n3 * sizeof(double)) M.U = gmgs::dalloc(n3 * sizeof(double));
     const auto t0 = Clock::now();
+    HostPrefault pf(U_host, 3 * (size_t)l0.n_node * sizeof(double));
+    M.ctx.trace_point("solve: start");
     const int st = gmgs::pcg_solve(M, M.F.as<double>(), M.U.as<double>(), iters, relres, hist);
+    M.ctx.trace_point("solve: PCG (incl. work buffers)");
     if (st == GMGS_ERR_NONFINITE) fail(st, "CG residual is not finite (diverged)");
     M.solved = true;
     const int64_t nn = l0.n_node;
@@ -109,9 +159,13 @@ int solve_impl(gmgs_handle* h, double* U_host, double* U_dev, int32_t* iters, do
             dst = tmp.as<double>();
         }
         gmgs::launch_dense_to_compact<double>(M.ctx, nn, l0.g.slots, l0.node_slot.as<int32_t>(), M.U.as<double>(), dst);
+        M.ctx.trace_point("solve: compaction");
+        pf.join();
+        M.ctx.trace_point("solve: host page prefault (join)");
         if (U_host)
             GMGS_CUDA(cudaMemcpyAsync(U_host, dst, 3 * nn * sizeof(double), cudaMemcpyDeviceToHost, M.ctx.stream));
         GMGS_CUDA(cudaStreamSynchronize(M.ctx.stream));
+        M.ctx.trace_point("solve: device-to-host copy");
     }
     M.t_solve_ms = ms_since(t0);
     if (st == GMGS_ERR_MAX_ITERATIONS) M.err = "Exceed the maximum iterate numbers";
@@ -208,11 +262,17 @@ int gmgs_create(const int32_t* occ, int32_t ny, int32_t nx, int32_t nz, const do
         GMGS_CUDA(cudaStreamCreateWithFlags(&M.ctx.stream, cudaStreamNonBlocking));
         M.own_stream = true;
         {
+            const char* tr = std::getenv("GMGS_TRACE");
+            M.ctx.trace = tr && tr[0] && tr[0] != '0';
+        }
+        M.ctx.trace_point("create: start");
+        {
             gmgs::DevBuf occ_dev = gmgs::dalloc((size_t)ny * nx * nz * sizeof(int32_t));
             GMGS_CUDA(cudaMemcpyAsync(occ_dev.p, occ, (size_t)ny * nx * nz * sizeof(int32_t), cudaMemcpyHostToDevice,
                                       M.ctx.stream));
             gmgs::build_levels(M, occ_dev.as<int32_t>());
         }
+        M.ctx.trace_point("create: occupancy buffer freed");
         gmgs::build_operators(M);
         M.ops_ready = true;
         M.t_create_ms = ms_since(t0);
@@ -226,7 +286,9 @@ int gmgs_set_bc(gmgs_handle* h, const int32_t* fixed, int64_t nfixed, const doub
         if (!h) fail(GMGS_ERR_INVALID_ARGUMENT, "handle is NULL");
         if (nload <= 0 || !loads) fail(GMGS_ERR_NO_LOADS, "No Loads! Unable to Perform Static FEA!");
         if (nfixed <= 0 || !fixed) fail(GMGS_ERR_NO_FIXINGS, "No Constraints! Unable to Perform Static FEA!");
+        h->M.ctx.trace_point("set_bc: start");
         gmgs::apply_bc(h->M, fixed, nfixed, loads, nload);
+        h->M.ctx.trace_point("set_bc: fixed nodes + loads");
         h->fixed_host.assign(fixed, fixed + nfixed);
         h->loads_host.assign(loads, loads + 4 * nload);
         h->M.bc_set = true;
@@ -279,7 +341,11 @@ static int stress_impl(gmgs_handle* h, double* nodal_host, float* vox_host, doub
     float* vd = vox_dev;
     if (nodal_host && !nd) { tn = gmgs::dalloc(6 * l0.n_node * sizeof(double)); nd = tn.as<double>(); }
     if (vox_host && !vd) { tv = gmgs::dalloc(6 * l0.n_elem * sizeof(float)); vd = tv.as<float>(); }
+    HostPrefault pfn(nodal_host, 6 * (size_t)l0.n_node * sizeof(double));
+    HostPrefault pfv(vox_host, 6 * (size_t)l0.n_elem * sizeof(float));
     gmgs::stress_dev(M, M.U.as<double>(), nd, vd);
+    pfn.join();
+    pfv.join();
     if (nodal_host)
         GMGS_CUDA(cudaMemcpyAsync(nodal_host, nd, 6 * l0.n_node * sizeof(double), cudaMemcpyDeviceToHost, M.ctx.stream));
     if (vox_host)
@@ -309,6 +375,7 @@ static int grad_impl(gmgs_handle* h, const double* ell_host, const double* ell_d
     if (!M.solved) fail(GMGS_ERR_NO_SOLUTION, "No Deformation Field Available, compute the deformation first");
     gmgs::Level& l0 = M.levels[0];
     const int64_t nn = l0.n_node, S = l0.g.slots;
+    HostPrefault pf(out_host, (size_t)l0.n_elem * sizeof(double));
     gmgs::DevBuf lam;
     const double* L = M.U.as<double>();
     if (ell_host || ell_dev) {
@@ -331,6 +398,7 @@ static int grad_impl(gmgs_handle* h, const double* ell_host, const double* ell_d
     double* od = out_dev;
     if (!od) { to = gmgs::dalloc(l0.n_elem * sizeof(double)); od = to.as<double>(); }
     gmgs::grad_dev(M, M.U.as<double>(), L, od);
+    pf.join();
     if (out_host)
         GMGS_CUDA(cudaMemcpyAsync(out_host, od, l0.n_elem * sizeof(double), cudaMemcpyDeviceToHost, M.ctx.stream));
     GMGS_CUDA(cudaStreamSynchronize(M.ctx.stream));

@@ -278,74 +278,128 @@ template void launch_fine<FM_CG_DIRECTION>(Ctx&, const FineLevel&, const Coef32&
 // x_f = (w r + P x_c) + w r', optionally the finest-level fixed DOFs zeroed
 // and the CG dot r . x_f accumulated (CG_solver.m:26).
 // ---------------------------------------------------------------------------
+// 32 x 8 node tiles, one thread per (iy, ix) column walking a chunk of z
+// planes; tiles without a solid node (k_tile_occ) are skipped.  The kernel is
+// bound by memory latency, so each thread keeps two fine planes in flight:
+// the flags, omega/diag, r and r' of plane z + 1 are loaded before plane z is
+// computed, and only solid nodes are written.  The four coarse values of a
+// coarse plane (Iy + {0,1}, Ix + {0,1}) stay in registers for the two fine
+// planes that use them (in-bounds: the halo covers Iy + 1, Ix + 1, Iz + 1).
 template <bool DOT>
-__global__ void __launch_bounds__(256) k_up32(Grid gf, Grid gc, const uint8_t* __restrict__ nflag,
+__global__ void __launch_bounds__(256, 4) k_up32(Grid gf, Grid gc, const uint8_t* __restrict__ nflag,
+                                              const uint8_t* __restrict__ tile_occ, int zc,
                                               const float* __restrict__ wdinv, const float* __restrict__ r,
                                               const float* __restrict__ rp, const float* __restrict__ xc,
                                               float* __restrict__ xf, int zero_fixed, DotOut dout) {
     __shared__ double sh[32];
     const int Sf = (int)gf.slots, Sc = (int)gc.slots;
-    const int csx = gc.py, csz = gc.py * gc.px;
-    const int ny1 = gf.ny + 1, nx1 = gf.nx + 1;
-    const int64_t total = (int64_t)ny1 * nx1 * (gf.nz + 1);
+    const int csx = gc.py, csz = gc.py * gc.px, fsz = gf.py * gf.px;
+    const int iy = blockIdx.x * TY + threadIdx.x, ix = blockIdx.y * TX + threadIdx.y;
+    const int zb = blockIdx.z * zc, ze = min(zb + zc, gf.nz + 1);
     Kahan dot;
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-        const int iy = (int)(t % ny1);
-        const int64_t rest = t / ny1;
-        const int ix = (int)(rest % nx1), iz = (int)(rest / nx1);
-        const int fs = (int)gf.slot(iy, ix, iz);
-        const uint8_t fl = nflag[fs];
-        if (!(fl & NF_SOLID)) continue;
-        const int Iy = iy >> 1, Ix = ix >> 1, Iz = iz >> 1;
-        const int oy = iy & 1, ox = ix & 1, oz = iz & 1;
-        const int c0 = (int)gc.slot(Iy, Ix, Iz);
-        const float w = (oy ? 0.5f : 1.f) * (ox ? 0.5f : 1.f) * (oz ? 0.5f : 1.f);
+    if (iy <= gf.ny && ix <= gf.nx) {
+        const int Iy = iy >> 1, Ix = ix >> 1;
+        const int oy = iy & 1, ox = ix & 1;
+        const float wyx = (oy ? 0.5f : 1.f) * (ox ? 0.5f : 1.f);
+        const int fcol = (int)gf.slot(iy, ix, 0), ccol = (int)gc.slot(Iy, Ix, 0);
+        const int64_t trow = (int64_t)gridDim.y * gridDim.x, tcol = (int64_t)blockIdx.y * gridDim.x + blockIdx.x;
+        auto occ = [&](int z) { return !tile_occ || tile_occ[z * trow + tcol] != 0; };
+        float qa[3][4], qb[3][4];
 #pragma unroll
-        for (int comp = 0; comp < 3; ++comp) {
-            const float* x = xc + comp * Sc;
-            float v = x[c0];
-            if (oy) v += x[c0 + 1];
-            if (ox) {
-                v += x[c0 + csx];
-                if (oy) v += x[c0 + csx + 1];
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) qa[c][k] = qb[c][k] = 0.f;
+        int qa_z = -1;
+        auto load_q = [&](int Z, float (&q)[3][4]) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float* x = xc + c * Sc + ccol + Z * csz;
+                q[c][0] = x[0]; q[c][1] = x[1]; q[c][2] = x[csx]; q[c][3] = x[csx + 1];
             }
-            if (oz) {
-                v += x[c0 + csz];
-                if (oy) v += x[c0 + csz + 1];
-                if (ox) {
-                    v += x[c0 + csz + csx];
-                    if (oy) v += x[c0 + csz + csx + 1];
+        };
+        uint8_t flc = 0, fln = 0;
+        float wdc[3] = {}, rc[3] = {}, rpc[3] = {}, wdn[3] = {}, rn[3] = {}, rpn[3] = {};
+        auto fetch = [&](int z, uint8_t& fl, float (&wd)[3], float (&rr)[3], float (&rq)[3]) {
+            const int fs = fcol + z * fsz;
+            fl = nflag[fs];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                wd[c] = wdinv[fs + c * Sf];
+                rr[c] = r[fs + c * Sf];
+                rq[c] = rp[fs + c * Sf];
+            }
+        };
+        bool okc = zb < ze && occ(zb);
+        if (okc) fetch(zb, flc, wdc, rc, rpc);
+        for (int iz = zb; iz < ze; ++iz) {
+            const bool okn = iz + 1 < ze && occ(iz + 1);
+            if (okn) fetch(iz + 1, fln, wdn, rn, rpn);
+            if (okc) {
+                const int Iz = iz >> 1, oz = iz & 1;
+                if (qa_z != Iz) { load_q(Iz, qa); qa_z = Iz; }
+                if (oz) load_q(Iz + 1, qb);
+                const float w = wyx * (oz ? 0.5f : 1.f);
+                if (flc & NF_SOLID) {
+                    const int fs = fcol + iz * fsz;
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        // the trilinear sum in a fixed order; absent terms add an exact zero
+                        float t = qa[c][0];
+                        t += oy ? qa[c][1] : 0.f;
+                        t += ox ? qa[c][2] : 0.f;
+                        t += (ox & oy) ? qa[c][3] : 0.f;
+                        t += oz ? qb[c][0] : 0.f;
+                        t += (oz & oy) ? qb[c][1] : 0.f;
+                        t += (oz & ox) ? qb[c][2] : 0.f;
+                        t += (oz & ox & oy) ? qb[c][3] : 0.f;
+                        float out = (wdc[c] * rc[c] + w * t) + wdc[c] * rpc[c];
+                        if (zero_fixed && (flc & (NF_FIX_X << c))) out = 0.f;
+                        xf[fs + c * Sf] = out;
+                        if (DOT) dot.add(rc[c] * out);
+                    }
+                }
+                if (oz) {
+#pragma unroll
+                    for (int c = 0; c < 3; ++c)
+#pragma unroll
+                        for (int k = 0; k < 4; ++k) qa[c][k] = qb[c][k];
+                    qa_z = Iz + 1;
                 }
             }
-            const int i = fs + comp * Sf;
-            const float wd = wdinv[i];
-            const float ri = r[i];
-            float out = (wd * ri + w * v) + wd * rp[i];
-            if (zero_fixed && (fl & (NF_FIX_X << comp))) out = 0.f;
-            xf[i] = out;
-            if (DOT) dot.add(ri * out);
+            flc = fln;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) { wdc[c] = wdn[c]; rc[c] = rn[c]; rpc[c] = rpn[c]; }
+            okc = okn;
         }
     }
     if (DOT) grid_dot_finish(dot.value(), dout, sh);
 }
 
-static int up32_blocks(const Ctx& c, const Grid& gf) {
-    const int64_t total = (int64_t)(gf.ny + 1) * (gf.nx + 1) * (gf.nz + 1);
-    return (int)std::max<int64_t>(1, std::min<int64_t>((total + 255) / 256, (int64_t)c.num_sms * 8));
+static int up32_zc(const Grid& g, const Ctx& c) {
+    const int64_t cols = (int64_t)((g.ny + 1 + TY - 1) / TY) * ((g.nx + 1 + TX - 1) / TX);
+    const int64_t want = (int64_t)c.num_sms * 4 * 8;      // ~8 waves of 4 resident CTAs per SM
+    return (int)std::min<int64_t>(64, std::max<int64_t>(2, (cols * (g.nz + 1) + want - 1) / want));
 }
 
-void launch_up32(Ctx& c, const Grid& gf, const Grid& gc, const uint8_t* nflag, const float* wdinv, const float* r,
-                 const float* rp, const float* xc, float* xf, bool zero_fixed, const DotOut* dot) {
-    const int blocks = up32_blocks(c, gf);
+void launch_up32(Ctx& c, const Grid& gf, const Grid& gc, const uint8_t* nflag, const uint8_t* tile_occ,
+                 const float* wdinv, const float* r, const float* rp, const float* xc, float* xf, bool zero_fixed,
+                 const DotOut* dot) {
+    const int zc = up32_zc(gf, c);
+    const dim3 grid((gf.ny + 1 + TY - 1) / TY, (gf.nx + 1 + TX - 1) / TX, (gf.nz + 1 + zc - 1) / zc);
+    const dim3 blk(TY, TX, 1);
     if (dot) {
-        k_up32<true><<<blocks, 256, 0, c.stream>>>(gf, gc, nflag, wdinv, r, rp, xc, xf, zero_fixed, *dot);
+        k_up32<true><<<grid, blk, 0, c.stream>>>(gf, gc, nflag, tile_occ, zc, wdinv, r, rp, xc, xf, zero_fixed, *dot);
     } else {
-        k_up32<false><<<blocks, 256, 0, c.stream>>>(gf, gc, nflag, wdinv, r, rp, xc, xf, zero_fixed, DotOut{});
+        k_up32<false><<<grid, blk, 0, c.stream>>>(gf, gc, nflag, tile_occ, zc, wdinv, r, rp, xc, xf, zero_fixed,
+                                                   DotOut{});
     }
     GMGS_LAUNCHED(c);
 }
 
-int up32_grid_blocks(const Grid& gf) { return 4096; }
+// upper bound of the k_up32 grid over the z-chunk choices (zc >= 2)
+int up32_grid_blocks(const Grid& g) {
+    return ((g.ny + 1 + TY - 1) / TY) * ((g.nx + 1 + TX - 1) / TX) * ((g.nz + 1 + 1) / 2);
+}
 
 // x -= the last, not yet cancelled Jacobi step dx = fl32(fl32(r32 - alpha q) * w)
 __global__ void k_drop_last_dx(int64_t n, double* __restrict__ x, const float* __restrict__ r32,

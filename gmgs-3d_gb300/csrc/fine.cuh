@@ -230,8 +230,9 @@ int up32_grid_blocks(const Grid& gf);
 template <int MODE>
 void launch_fine(Ctx& c, const FineLevel& L, const Coef32& cf, const FineArgs& a);
 
-void launch_up32(Ctx& c, const Grid& gf, const Grid& gc, const uint8_t* nflag, const float* wdinv, const float* r,
-                 const float* rp, const float* xc, float* xf, bool zero_fixed, const DotOut* dot);
+void launch_up32(Ctx& c, const Grid& gf, const Grid& gc, const uint8_t* nflag, const uint8_t* tile_occ,
+                 const float* wdinv, const float* r, const float* rp, const float* xc, float* xf, bool zero_fixed,
+                 const DotOut* dot);
 void launch_wdinv(Ctx& c, int64_t n, const double* d, double omega, float* w);
 void launch_perel_vdown(Ctx& c, const FineLevel& L, const Coef32& cf, const int32_t* nodes, int count, const float* r,
                         const float* w, float* out);

@@ -16,6 +16,7 @@
 
 #include <cuda_runtime.h>
 #include <atomic>
+#include <chrono>
 #include <cstdint>
 #include <cstdio>
 #include <stdexcept>
@@ -194,6 +195,19 @@ struct Ctx {
     int num_sms = 148;
     bool prof = false;
     ProfSlot prof_slot[PK_COUNT];
+    // Setup/solve phase trace on stderr (environment GMGS_TRACE=1): each
+    // point waits for the stream and prints the wall time since the last one.
+    bool trace = false;
+    std::chrono::steady_clock::time_point t_trace{};
+    void trace_point(const char* what) {
+        if (!trace) return;
+        cudaStreamSynchronize(stream);
+        const auto now = std::chrono::steady_clock::now();
+        if (t_trace.time_since_epoch().count())
+            std::fprintf(stderr, "[gmgs] %-34s %9.3f ms\n", what,
+                         std::chrono::duration<double, std::milli>(now - t_trace).count());
+        t_trace = now;
+    }
     // record a start (stop=false) or stop event for kernel k
     void mark(int k, bool stop, double bytes = 0) {
         if (!prof) return;

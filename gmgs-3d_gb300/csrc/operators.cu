@@ -162,7 +162,7 @@ __device__ __forceinline__ bool complement_ok(const LevelView<Tc>& lv, int64_t n
             if (lv.etype && lv.etype[es] > 0) return false;
         }
     }
-    return solid >= 4;
+    return solid >= 6;
 }
 
 // rows of corner c of the uniform element at es, times s (run-time corner)
@@ -198,9 +198,10 @@ __global__ void __launch_bounds__(128) k_matvec(LevelView<Tc> lv, const __grid_c
         interior_pairs<Tc, Tin>(cf, x, n, S, sx, sz, a0, a1, a2);
         a0 *= kscale; a1 *= kscale; a2 *= kscale;
     } else if ((f & NF_SOLID) && complement_ok(lv, n, sx, sz)) {
-        // all solid elements uniform, at most four void: the assembled stencil
-        // minus the void elements' rows costs fewer operations than the solid
-        // elements' rows (AtX.m:34-56 sums the latter)
+        // all solid elements uniform, at most two void: the assembled stencil
+        // (≈160 FMA) minus the void elements' rows (72 each) costs fewer
+        // operations than the solid elements' rows (AtX.m:34-56 sums the
+        // latter, 72 each); with three or four void elements it does not
         interior_pairs<Tc, Tin>(cf, x, n, S, sx, sz, a0, a1, a2);
         a0 *= kscale; a1 *= kscale; a2 *= kscale;
 #pragma unroll 1

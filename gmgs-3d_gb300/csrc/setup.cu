@@ -683,8 +683,10 @@ void build_levels(Model& M, const int32_t* occ_dev) {
         k_etype<<<blocks_for(c, lv.g.slots), 256, 0, c.stream>>>(
             lv.g.slots, lv.emask.as<uint8_t>(), need.as<int32_t>(), need0.as<int32_t>(), lv.etype.as<int32_t>(),
             lv.kslot.as<int32_t>());
-        GMGS_LAUNCHED(c);        GMGS_CUDA(cudaStreamSynchronize(c.stream));   // temporaries are freed at scope exit
+        GMGS_LAUNCHED(c);
+        GMGS_CUDA(cudaStreamSynchronize(c.stream));   // temporaries are freed at scope exit
     }
+    c.trace_point("create: coarse masks + matrix selection");
     // node flags, compact node maps, element counts
     for (int l = 0; l < L; ++l) {
         Level& lv = M.levels[l];
@@ -713,6 +715,7 @@ void build_levels(Model& M, const int32_t* occ_dev) {
     }
     if (M.levels[0].n_elem == 0) throw Error(GMGS_ERR_NO_SOLID, "the occupancy has no solid voxel");
     GMGS_CUDA(cudaStreamSynchronize(c.stream));
+    c.trace_point("create: node/element lists");
 }
 
 __global__ void k_escale(int64_t ne, const int32_t* __restrict__ elem_slot, const double* __restrict__ rho,
@@ -770,6 +773,7 @@ void build_operators(Model& M) {
             GMGS_CUDA(cudaStreamSynchronize(c.stream));
         }
     }
+    c.trace_point("create: interior flags");
     M.ke0_dev = dalloc(KE * sizeof(double));
     GMGS_CUDA(cudaMemcpyAsync(M.ke0_dev.p, KeT, KE * sizeof(double), cudaMemcpyHostToDevice, c.stream));
     const double* ke0 = M.ke0_dev.as<double>();
@@ -845,6 +849,7 @@ void build_operators(Model& M) {
             GMGS_LAUNCHED(c);
         }
     }
+    c.trace_point("create: Galerkin coarse matrices");
     // diagonals (levels 1..L-1) and FP32 copies for the mixed V-cycle
     for (int l = 0; l < L; ++l) {
         Level& lv = M.levels[l];
@@ -884,6 +889,7 @@ void build_operators(Model& M) {
         }
     }
     GMGS_CUDA(cudaStreamSynchronize(c.stream));
+    c.trace_point("create: diagonals + FP32 copies");
 }
 
 void apply_bc(Model& M, const int32_t* fixed, int64_t nfixed, const double* loads, int64_t nload) {
@@ -954,6 +960,7 @@ void build_coarse_bc(Model& M) {
         GMGS_CUDA(cudaStreamSynchronize(c.stream));
         ind = std::move(indc);
     }
+    c.trace_point("bc: restricted fixed indicator");
     // coarsest free DOFs, dense K, Cholesky, inverse
     Level& lc = M.levels[L - 1];
     const int64_t S = lc.g.slots;
@@ -979,6 +986,7 @@ void build_coarse_bc(Model& M) {
         lc.g, (int)nf, M.free_idx.as<int32_t>(), rank.as<int32_t>(), lc.emask.as<uint8_t>(), lc.etype.as<int32_t>(),
         lc.Ks64.as<double>(), M.ke0_dev.as<double>(), lc.kscale, M.kinv.as<double>());
     GMGS_LAUNCHED(c);
+    c.trace_point("bc: coarsest free DOFs + assembly");
     // Kd is row-major K[row][col]; cuSOLVER is column-major, so it sees K^T = K.
     // potrf factors K = L L^T into the column-major lower triangle and trtri
     // replaces L by Linv = L^-1 there (row-major: the upper triangle holds
@@ -1054,7 +1062,9 @@ void build_coarse_bc(Model& M) {
                                &one, blk(i + 1, i + 1), n), "cublasDsyrk");
             }
         }
+        c.trace_point("bc: block Cholesky");
         for (int i = 0; i < nb; ++i) trtri(bsz(i), blk(i, i), infos + 2 * i + 1);
+        c.trace_point("bc: diagonal block inverses");
         DevBuf T = dalloc((size_t)B * n * sizeof(double));
         double* t = T.as<double>();
         for (int i = 1; i < nb; ++i) {                  // block row i of Linv
@@ -1070,6 +1080,7 @@ void build_coarse_bc(Model& M) {
                            w0 + bp, &mone, blk(i, i), n, t, bi, blk(i, 0), n), "cublasDtrmm");
         }
         GMGS_CUDA(cudaStreamSynchronize(c.stream));
+        c.trace_point("bc: inverse factor block rows");
     }
     std::vector<int> hinfo(2 * std::max(1, nb));
     GMGS_CUDA(cudaMemcpyAsync(hinfo.data(), info.p, hinfo.size() * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
@@ -1084,6 +1095,7 @@ void build_coarse_bc(Model& M) {
     M.cvec_in = dalloc(nf * sizeof(double));
     M.cvec_out = dalloc(nf * sizeof(double));
     GMGS_CUDA(cudaStreamSynchronize(c.stream));
+    c.trace_point("bc: symmetrise + vectors");
 }
 
 }  // namespace gmgs

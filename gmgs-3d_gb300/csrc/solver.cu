@@ -216,7 +216,8 @@ static void vcycle32(Model& M, const float* r32, float* z, bool with_dot, int do
             c.mark(PK_COARSE, true);
             c.mark(PK_UP0, false);
         }
-        launch_up32(c, lv.g, M.levels[l + 1].g, lv.nflag.as<uint8_t>(), lv.wdinv32.as<float>(),
+        launch_up32(c, lv.g, M.levels[l + 1].g, lv.nflag.as<uint8_t>(), lv.tile_occ.as<uint8_t>(),
+                    lv.wdinv32.as<float>(),
                     l == 0 ? r32 : lv.vr.as<float>(), lv.vrp.as<float>(), M.levels[l + 1].vx.as<float>(),
                     l == 0 ? z : lv.vx.as<float>(), l == 0, (l == 0 && with_dot) ? &d : nullptr);
         if (l == 0) c.mark(PK_UP0, true, (double)lv.n_node * 3 * 20);

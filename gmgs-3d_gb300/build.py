@@ -20,7 +20,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = ROOT / "_build" / "gmgs"
 LIB = PKG / "gmgs" / "libgmgs.so"
-SOURCES = ["api.cu", "setup.cu", "operators.cu", "solver.cu", "post.cu", "fine.cu", "noalloc.cu", "voxelize.cu"]
+SOURCES = ["api.cu", "setup.cu", "operators.cu", "solver.cu", "post.cu", "fine.cu", "noalloc.cu", "voxelize.cu", "coarse.cu"]
 # the voxeliser decides inside/outside by exact FP64 comparisons: no FMA contraction
 FILE_FLAGS = {"voxelize.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -63,7 +63,7 @@ def build(debug: bool = False, jobs: int | None = None) -> Path:
     newest = max(o.stat().st_mtime for o in objs)
     if LIB.exists() and LIB.stat().st_mtime >= newest and not debug:
         return LIB
-    cmd = [nvcc(), *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcusolver", "-lcublas", "-lcudart"]
+    cmd = [nvcc(), *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcudart"]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")

@@ -130,7 +130,7 @@ int64_t model_bytes(const gmgs::Model& M) {
                                       &lv.kslot, &lv.diag64, &lv.diag32, &lv.wdinv32, &lv.emask8, &lv.perel_nodes, &lv.node_slot, &lv.elem_slot,
                                       &lv.vr, &lv.vrp, &lv.vdx, &lv.vx, &lv.vy, &lv.tile_occ})
             b += (int64_t)d->bytes;
-    for (const gmgs::DevBuf* d : {&M.ke0_dev, &M.rho, &M.F, &M.U, &M.free_idx, &M.kinv, &M.cvec_in, &M.cvec_tmp, &M.cvec_out,
+    for (const gmgs::DevBuf* d : {&M.ke0_dev, &M.rho, &M.F, &M.U, &M.free_idx, &M.cb.sinv, &M.cb.g, &M.cb.partial, &M.cb.ticket, &M.cvec_in, &M.cvec_out,
                                   &M.cg_x, &M.cg_r, &M.cg_p, &M.cg_dx, &M.cg_q64, &M.cg_y64, &M.cg_z64, &M.cg_q32,
                                   &M.cg_y32, &M.cg_z32, &M.cg_r32, &M.cg_r32b, &M.cg_pa, &M.cg_pb, &M.scal, &M.dot_partials, &M.dot_ticket})
         b += (int64_t)d->bytes;
@@ -270,6 +270,7 @@ int gmgs_create(const int32_t* occ, int32_t ny, int32_t nx, int32_t nz, const do
             gmgs::DevBuf occ_dev = gmgs::dalloc((size_t)ny * nx * nz * sizeof(int32_t));
             GMGS_CUDA(cudaMemcpyAsync(occ_dev.p, occ, (size_t)ny * nx * nz * sizeof(int32_t), cudaMemcpyHostToDevice,
                                       M.ctx.stream));
+            M.ctx.trace_point("create: occupancy to device");
             gmgs::build_levels(M, occ_dev.as<int32_t>());
         }
         M.ctx.trace_point("create: occupancy buffer freed");

@@ -290,7 +290,21 @@ template <typename T>
 void launch_gather(Ctx& c, int64_t n, const int32_t* idx, const T* src, double* dst);
 template <typename T>
 void launch_scatter(Ctx& c, int64_t n, const int32_t* idx, const double* src, T* dst);
-void launch_coarse_solve(Ctx& c, int n, const double* kinv, const double* r, double* tmp, double* z);
+// coarsest level: block-tridiagonal LDL^T of the free-DOF matrix, factored
+// from both ends towards the middle block (coarse.cu)
+struct CoarseBlocks {
+    int n = 0;        // free DOFs
+    int B = 0;        // block order: a multiple of 64, at least the half bandwidth
+    int nb = 0;       // blocks; rows n..nb*B-1 are identity padding
+    DevBuf sinv;      // nb x (B x B) column-major: A_ii on entry, D_i^-1 after factor_coarse
+    DevBuf g;         // nb x (B x B): A_(i,i-1) on entry, the coupling G_i or H_(i-1) after
+    DevBuf partial;   // max(nb, 4) x (B/64) x B partial sums of the block matrix-vector products
+    DevBuf ticket;    // max(nb, 4) arrival counters (zero between launches)
+};
+int coarse_block_order(int n, int half_bandwidth);
+void factor_coarse(Ctx& c, CoarseBlocks& cb);
+// x = A^-1 r: r in cvec (overwritten), both nb*B long with zero padding
+void launch_coarse_solve(Ctx& c, const CoarseBlocks& cb, double* cvec, double* x);
 
 // compact <-> dense (interleaved 3-vectors)
 template <typename T>

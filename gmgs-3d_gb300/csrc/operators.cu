@@ -548,31 +548,6 @@ template void launch_gather<float>(Ctx&, int64_t, const int32_t*, const float*, 
 template void launch_scatter<double>(Ctx&, int64_t, const int32_t*, const double*, double*);
 template void launch_scatter<float>(Ctx&, int64_t, const int32_t*, const double*, float*);
 
-// coarsest solve z = K^-1 r = Linv^T (Linv r) with kinv[i][j] = Linv[i][j]
-// for j <= i and Linv[j][i] for j >= i: one warp per row, the lower sweep
-// reads columns 0..i of row i, the upper sweep columns i..n-1
-template <bool LOWER>
-__global__ void __launch_bounds__(256) k_trimv(int n, const double* __restrict__ A, const double* __restrict__ x,
-                                               double* __restrict__ y) {
-    const int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    const int lane = threadIdx.x & 31;
-    if (row >= n) return;
-    const double* a = A + (int64_t)row * n;
-    const int j0 = LOWER ? 0 : row, j1 = LOWER ? row + 1 : n;
-    double s = 0;
-    for (int j = j0 + lane; j < j1; j += 32) s += a[j] * x[j];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    if (lane == 0) y[row] = s;
-}
-void launch_coarse_solve(Ctx& c, int n, const double* kinv, const double* r, double* tmp, double* z) {
-    if (n <= 0) return;
-    k_trimv<true><<<(n + 7) / 8, 256, 0, c.stream>>>(n, kinv, r, tmp);
-    GMGS_LAUNCHED(c);
-    k_trimv<false><<<(n + 7) / 8, 256, 0, c.stream>>>(n, kinv, tmp, z);
-    GMGS_LAUNCHED(c);
-}
-
 // ---------------------------------------------------------------------------
 // compact interleaved <-> dense planes
 // ---------------------------------------------------------------------------

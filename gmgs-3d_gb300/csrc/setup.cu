@@ -6,8 +6,6 @@
 // src/kernel/BuildingMeshHierarchy.m:8-142, src/kernel/SetupSolver.m:9-259,
 // src/kernel/DirectlyAssembleStifnessMatrix.m:24-34,
 // src/common/ApplyBoundaryCondition.m:7-23.
-#include <cublas_v2.h>
-#include <cusolverDn.h>
 
 #include <algorithm>
 #include <cmath>
@@ -568,66 +566,89 @@ __global__ void k_free_list(int64_t S, const uint8_t* __restrict__ f, const int3
 // row = dof of local i, col = dof of local j (DirectlyAssembleStifnessMatrix.m:25-32).
 // Stored matrices have row = output DOF, so Ks_e(i, j) = M_e[j][i].
 // One thread per (free row, neighbour dof); deterministic element order.
-__global__ void k_assemble_coarsest(Grid g, int nf, const int32_t* __restrict__ freeidx, const int32_t* __restrict__ rank,
-                                    const uint8_t* __restrict__ emask, const int32_t* __restrict__ etype,
-                                    const double* __restrict__ Ks, const double* __restrict__ ke0, double kscale,
-                                    double* __restrict__ Kd) {
-    const int64_t total = (int64_t)nf * 81;
-    GRID_STRIDE(t, total) {
-        const int row = (int)(t / 81);
-        const int k = (int)(t % 81);
-        const int off = k / 3, be = k % 3;
-        const int oa = off % 3 - 1, ob = (off / 3) % 3 - 1, oc = off / 9 - 1;
-        const int64_t ri = freeidx[row];
-        const int64_t S = g.slots;
-        const int al = (int)(ri / S);
-        const int64_t n = ri % S;
-        const int64_t m = n + oa + ob * g.sx() + oc * g.sz();
-        const int col = rank[m + be * S];
-        if (col < 0) continue;
-        double v = 0;
-        for (int e = 0; e < 8; ++e) {
-            const int A = e & 1, B = (e >> 1) & 1, C = e >> 2;
-            const int64_t es = n - A - B * g.sx() - C * g.sz();
-            // element must also contain m: m - es in {0,1}^3
-            const int my = A + oa, mx = B + ob, mz = C + oc;
-            if (my < 0 || my > 1 || mx < 0 || mx > 1 || mz < 0 || mz > 1) continue;
-            if (!emask[es]) continue;
-            const int cn = corner_of(A, B, C), cm = corner_of(my, mx, mz);
-            const int t2 = etype ? etype[es] : 0;
-            const int ii = (3 * cm + be) * 24 + 3 * cn + al;
-            v += t2 > 0 ? Ks[(int64_t)(t2 - 1) * KE + ii] : kscale * ke0[ii];
-        }
-        Kd[(int64_t)row * nf + col] = v;
+// Entry t = (row, k) of the coarsest free-DOF matrix: row = free DOF, k =
+// (neighbour offset, component) of the column; the value sums the
+// contributions of the solid elements shared by the two nodes
+// (DirectlyAssembleStifnessMatrix.m:24-34 restricted to the free DOFs).
+// Returns false when the column DOF is fixed or outside the level.
+__device__ __forceinline__ bool coarse_entry(const Grid& g, int64_t t, const int32_t* __restrict__ freeidx,
+                                             const int32_t* __restrict__ rank, const uint8_t* __restrict__ emask,
+                                             const int32_t* __restrict__ etype, const double* __restrict__ Ks,
+                                             const double* __restrict__ ke0, double kscale, int& row, int& col,
+                                             double& v) {
+    row = (int)(t / 81);
+    const int k = (int)(t % 81);
+    const int off = k / 3, be = k % 3;
+    const int oa = off % 3 - 1, ob = (off / 3) % 3 - 1, oc = off / 9 - 1;
+    const int64_t ri = freeidx[row];
+    const int64_t S = g.slots;
+    const int al = (int)(ri / S);
+    const int64_t n = ri % S;
+    const int64_t m = n + oa + ob * g.sx() + oc * g.sz();
+    col = rank[m + be * S];
+    if (col < 0) return false;
+    v = 0;
+    for (int e = 0; e < 8; ++e) {
+        const int A = e & 1, B = (e >> 1) & 1, C = e >> 2;
+        const int64_t es = n - A - B * g.sx() - C * g.sz();
+        // element must also contain m: m - es in {0,1}^3
+        const int my = A + oa, mx = B + ob, mz = C + oc;
+        if (my < 0 || my > 1 || mx < 0 || mx > 1 || mz < 0 || mz > 1) continue;
+        if (!emask[es]) continue;
+        const int cn = corner_of(A, B, C), cm = corner_of(my, mx, mz);
+        const int t2 = etype ? etype[es] : 0;
+        const int ii = (3 * cm + be) * 24 + 3 * cn + al;
+        v += t2 > 0 ? Ks[(int64_t)(t2 - 1) * KE + ii] : kscale * ke0[ii];
     }
+    return true;
+}
+
+// half bandwidth: max |col - row| over non-zero entries
+__global__ void k_coarse_bandwidth(Grid g, int nf, const int32_t* __restrict__ freeidx,
+                                   const int32_t* __restrict__ rank, const uint8_t* __restrict__ emask,
+                                   const int32_t* __restrict__ etype, const double* __restrict__ Ks,
+                                   const double* __restrict__ ke0, double kscale, int* __restrict__ bw) {
+    int best = 0;
+    GRID_STRIDE(t, (int64_t)nf * 81) {
+        int row, col;
+        double v;
+        if (coarse_entry(g, t, freeidx, rank, emask, etype, Ks, ke0, kscale, row, col, v) && v != 0.0)
+            best = max(best, col > row ? col - row : row - col);
+    }
+    for (int o = 16; o > 0; o >>= 1) best = max(best, __shfl_xor_sync(0xffffffffu, best, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(bw, best);
+}
+
+// the diagonal blocks A_ii (both triangles) and sub-diagonal blocks
+// A_(i,i-1) of the block-tridiagonal form, column-major B x B
+__global__ void k_assemble_blocks(Grid g, int nf, const int32_t* __restrict__ freeidx,
+                                  const int32_t* __restrict__ rank, const uint8_t* __restrict__ emask,
+                                  const int32_t* __restrict__ etype, const double* __restrict__ Ks,
+                                  const double* __restrict__ ke0, double kscale, int B, double* __restrict__ diag,
+                                  double* __restrict__ sub) {
+    const int64_t B2 = (int64_t)B * B;
+    GRID_STRIDE(t, (int64_t)nf * 81) {
+        int row, col;
+        double v;
+        if (!coarse_entry(g, t, freeidx, rank, emask, etype, Ks, ke0, kscale, row, col, v)) continue;
+        const int bi = row / B, bj = col / B;
+        const int64_t at = (int64_t)(row % B) + (int64_t)(col % B) * B;
+        if (bi == bj) diag[bi * B2 + at] = v;
+        else if (bi == bj + 1) sub[bi * B2 + at] = v;
+    }
+}
+
+// identity on the padding rows of the last diagonal block
+__global__ void k_pad_identity(int n, int npad, int B, double* __restrict__ diag) {
+    const int i = n + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= npad) return;
+    const int64_t B2 = (int64_t)B * B;
+    diag[(int64_t)(i / B) * B2 + (int64_t)(i % B) * (B + 1)] = 1.0;
 }
 __global__ void k_rank_fill(int64_t n, int32_t* r) { GRID_STRIDE(i, n) r[i] = -1; }
 __global__ void k_rank_set(int64_t nf, const int32_t* __restrict__ idx, int32_t* __restrict__ r) {
     GRID_STRIDE(i, nf) r[idx[i]] = (int32_t)i;
 }
-__global__ void k_symmetrize_lower(int n, double* A) {
-    const int64_t total = (int64_t)n * n;
-    GRID_STRIDE(t, total) {
-        const int i = (int)(t / n), j = (int)(t % n);
-        // column-major lower (i >= j) holds the result; write the upper mirror
-        if (i < j) A[(int64_t)j * n + i] = A[(int64_t)i * n + j];
-    }
-}
-
-// half bandwidth of the assembled coarsest matrix: max (col - row) over
-// non-zeros; one warp per row, coalesced
-__global__ void k_bandwidth(int n, const double* __restrict__ A, int* __restrict__ bw) {
-    const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (w >= n) return;
-    const double* row = A + w * (int64_t)n;
-    int last = (int)w;
-    for (int c = (int)w + lane; c < n; c += 32)
-        if (row[c] != 0.0) last = c;
-    for (int o = 16; o > 0; o >>= 1) last = max(last, __shfl_xor_sync(0xffffffffu, last, o));
-    if (lane == 0) atomicMax(bw, last - (int)w);
-}
-
 __global__ void k_to_float(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
     GRID_STRIDE(i, n) b[i] = (float)a[i];
 }
@@ -659,6 +680,7 @@ void build_levels(Model& M, const int32_t* occ_dev) {
                                                                      lv.emask.as<uint8_t>());
         GMGS_LAUNCHED(c);
     }
+    c.trace_point("create: level buffers + finest mask");
     // coarse masks + per-element matrix selection
     for (int l = 1; l < L; ++l) {
         Level& lv = M.levels[l];
@@ -961,7 +983,7 @@ void build_coarse_bc(Model& M) {
         ind = std::move(indc);
     }
     c.trace_point("bc: restricted fixed indicator");
-    // coarsest free DOFs, dense K, Cholesky, inverse
+    // coarsest free DOFs and their block-tridiagonal factorisation
     Level& lc = M.levels[L - 1];
     const int64_t S = lc.g.slots;
     DevBuf cnt = dalloc(3 * S * sizeof(int32_t));
@@ -969,7 +991,6 @@ void build_coarse_bc(Model& M) {
     GMGS_LAUNCHED(c);
     const int64_t nf = exclusive_scan(c, cnt.as<int32_t>(), 3 * S);
     if (nf == 0) throw Error(GMGS_ERR_NOT_SPD, "no free DOFs on the coarsest level");
-    if (nf > 40000) throw Error(GMGS_ERR_RESOLUTION, "coarsest level too large for a dense factorisation; use more levels");
     M.nfree = (int)nf;
     M.free_idx = dalloc(nf * sizeof(int32_t));
     k_free_list<<<blocks_for(c, 3 * S), 256, 0, c.stream>>>(S, lc.nflag.as<uint8_t>(), cnt.as<int32_t>(),
@@ -980,122 +1001,50 @@ void build_coarse_bc(Model& M) {
     GMGS_LAUNCHED(c);
     k_rank_set<<<blocks_for(c, nf), 256, 0, c.stream>>>(nf, M.free_idx.as<int32_t>(), rank.as<int32_t>());
     GMGS_LAUNCHED(c);
-    M.kinv = dalloc((size_t)nf * nf * sizeof(double));
-    GMGS_CUDA(cudaMemsetAsync(M.kinv.p, 0, (size_t)nf * nf * sizeof(double), c.stream));
-    k_assemble_coarsest<<<blocks_for(c, nf * 81), 256, 0, c.stream>>>(
-        lc.g, (int)nf, M.free_idx.as<int32_t>(), rank.as<int32_t>(), lc.emask.as<uint8_t>(), lc.etype.as<int32_t>(),
-        lc.Ks64.as<double>(), M.ke0_dev.as<double>(), lc.kscale, M.kinv.as<double>());
-    GMGS_LAUNCHED(c);
-    c.trace_point("bc: coarsest free DOFs + assembly");
-    // Kd is row-major K[row][col]; cuSOLVER is column-major, so it sees K^T = K.
-    // potrf factors K = L L^T into the column-major lower triangle and trtri
-    // replaces L by Linv = L^-1 there (row-major: the upper triangle holds
-    // Linv^T).  Mirroring it into the row-major lower triangle gives
-    //   kinv[i][j] = Linv[i][j] (j <= i),  kinv[i][j] = Linv[j][i] (j >= i),
-    // so K^-1 r = Linv^T (Linv r) is two half-row sweeps (launch_coarse_solve).
-    // Forming Linv instead of K^-1 (potri) skips the L^-T L^-1 product.
-    cusolverDnHandle_t hs = nullptr;
-    if (cusolverDnCreate(&hs) != CUSOLVER_STATUS_SUCCESS) throw Error(GMGS_ERR_CUDA, "cusolverDnCreate failed");
-    struct Guard { cusolverDnHandle_t h; ~Guard() { cusolverDnDestroy(h); } } guard{hs};
-    cusolverDnSetStream(hs, c.stream);
+    // The free DOFs are numbered node by node in slot order, so the matrix is
+    // banded: blocks of order B >= the half bandwidth make it block
+    // tridiagonal (factor_coarse, coarse.cu).
     const int n = (int)nf;
-    double* A = M.kinv.as<double>();
-    // The free DOFs are numbered node by node in slot order, so K is banded:
-    // with blocks at least as wide as the half bandwidth it is block
-    // tridiagonal, its Cholesky factor block bidiagonal (block potrf / trsm /
-    // syrk), and the inverse factor follows block row by block row from
-    //   Linv_ii = L_ii^-1,  Linv_ij = -Linv_ii C_i Linv_(i-1)j  (j < i),
-    // C_i the sub-diagonal block of L: about a quarter of the flops of dense
-    // potrf + trtri, with the same result in the same place.
     int bw = 0;
     {
         DevBuf dbw = dalloc(sizeof(int));
         GMGS_CUDA(cudaMemsetAsync(dbw.p, 0, sizeof(int), c.stream));
-        k_bandwidth<<<(unsigned)(((int64_t)n * 32 + 255) / 256), 256, 0, c.stream>>>(n, A, dbw.as<int>());
+        k_coarse_bandwidth<<<blocks_for(c, (int64_t)n * 81), 256, 0, c.stream>>>(
+            lc.g, n, M.free_idx.as<int32_t>(), rank.as<int32_t>(), lc.emask.as<uint8_t>(), lc.etype.as<int32_t>(),
+            lc.Ks64.as<double>(), M.ke0_dev.as<double>(), lc.kscale, dbw.as<int>());
         GMGS_LAUNCHED(c);
         GMGS_CUDA(cudaMemcpyAsync(&bw, dbw.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
         GMGS_CUDA(cudaStreamSynchronize(c.stream));
     }
-    const int B = std::max(32, (bw + 31) / 32 * 32);
-    const int nb = (n + B - 1) / B;
-    auto bsz = [&](int i) { return std::min(B, n - i * B); };
-    const int fmax = nb >= 3 ? B : n;                 // largest potrf / trtri order
-    int lwork = 0;
-    size_t tw_dev = 0, tw_host = 0;
-    if (cusolverDnDpotrf_bufferSize(hs, CUBLAS_FILL_MODE_LOWER, fmax, A, n, &lwork) != CUSOLVER_STATUS_SUCCESS ||
-        cusolverDnXtrtri_bufferSize(hs, CUBLAS_FILL_MODE_LOWER, CUBLAS_DIAG_NON_UNIT, fmax, CUDA_R_64F, A, n, &tw_dev,
-                                    &tw_host) != CUSOLVER_STATUS_SUCCESS)
-        throw Error(GMGS_ERR_CUDA, "cuSOLVER buffer size query failed");
-    DevBuf work = dalloc(std::max((size_t)lwork * sizeof(double), tw_dev));
-    std::vector<unsigned char> hwork(std::max<size_t>(1, tw_host));
-    DevBuf info = dalloc(2 * sizeof(int) * std::max(1, nb));
-    GMGS_CUDA(cudaMemsetAsync(info.p, 0, 2 * sizeof(int) * std::max(1, nb), c.stream));
-    auto potrf = [&](int m, double* a, int* inf) {
-        if (cusolverDnDpotrf(hs, CUBLAS_FILL_MODE_LOWER, m, a, n, work.as<double>(), lwork, inf) != CUSOLVER_STATUS_SUCCESS)
-            throw Error(GMGS_ERR_CUDA, "cusolverDnDpotrf failed");
-    };
-    auto trtri = [&](int m, double* a, int* inf) {
-        if (cusolverDnXtrtri(hs, CUBLAS_FILL_MODE_LOWER, CUBLAS_DIAG_NON_UNIT, m, CUDA_R_64F, a, n, work.p, tw_dev,
-                             hwork.data(), tw_host, inf) != CUSOLVER_STATUS_SUCCESS)
-            throw Error(GMGS_ERR_CUDA, "cusolverDnXtrtri failed");
-    };
-    int* infos = info.as<int>();
-    if (nb < 3) {
-        potrf(n, A, infos);
-        trtri(n, A, infos + 1);
-    } else {
-        cublasHandle_t hb = nullptr;
-        if (cublasCreate(&hb) != CUBLAS_STATUS_SUCCESS) throw Error(GMGS_ERR_CUDA, "cublasCreate failed");
-        struct BGuard { cublasHandle_t h; ~BGuard() { cublasDestroy(h); } } bguard{hb};
-        cublasSetStream(hb, c.stream);
-        auto ok = [](cublasStatus_t st, const char* what) {
-            if (st != CUBLAS_STATUS_SUCCESS) throw Error(GMGS_ERR_CUDA, std::string(what) + " failed");
-        };
-        const double one = 1.0, mone = -1.0, zero = 0.0;
-        auto blk = [&](int bi, int bj) { return A + (int64_t)bi * B + (int64_t)bj * B * n; };   // column-major block
-        for (int i = 0; i < nb; ++i) {                  // block Cholesky, column-major lower
-            potrf(bsz(i), blk(i, i), infos + 2 * i);
-            if (i + 1 < nb) {
-                ok(cublasDtrsm(hb, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT,
-                               bsz(i + 1), bsz(i), &one, blk(i, i), n, blk(i + 1, i), n), "cublasDtrsm");
-                ok(cublasDsyrk(hb, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, bsz(i + 1), bsz(i), &mone, blk(i + 1, i), n,
-                               &one, blk(i + 1, i + 1), n), "cublasDsyrk");
-            }
-        }
-        c.trace_point("bc: block Cholesky");
-        for (int i = 0; i < nb; ++i) trtri(bsz(i), blk(i, i), infos + 2 * i + 1);
-        c.trace_point("bc: diagonal block inverses");
-        DevBuf T = dalloc((size_t)B * n * sizeof(double));
-        double* t = T.as<double>();
-        for (int i = 1; i < nb; ++i) {                  // block row i of Linv
-            const int bi = bsz(i), bp = bsz(i - 1), w0 = (i - 1) * B;
-            if (w0 > 0)                                 // T[:, 0:w0] = C_i Linv[i-1, 0:w0]
-                ok(cublasDgemm(hb, CUBLAS_OP_N, CUBLAS_OP_N, bi, w0, bp, &one, blk(i, i - 1), n, blk(i - 1, 0), n,
-                               &zero, t, bi), "cublasDgemm");
-            // T[:, w0:w0+bp] = C_i Linv[i-1, i-1] (lower triangular)
-            ok(cublasDtrmm(hb, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, bi, bp,
-                           &one, blk(i - 1, i - 1), n, blk(i, i - 1), n, t + (int64_t)w0 * bi, bi), "cublasDtrmm");
-            // Linv[i, 0:w0+bp] = -Linv_ii T
-            ok(cublasDtrmm(hb, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, bi,
-                           w0 + bp, &mone, blk(i, i), n, t, bi, blk(i, 0), n), "cublasDtrmm");
-        }
-        GMGS_CUDA(cudaStreamSynchronize(c.stream));
-        c.trace_point("bc: inverse factor block rows");
-    }
-    std::vector<int> hinfo(2 * std::max(1, nb));
-    GMGS_CUDA(cudaMemcpyAsync(hinfo.data(), info.p, hinfo.size() * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
-    GMGS_CUDA(cudaStreamSynchronize(c.stream));
-    for (size_t k = 0; k < hinfo.size(); k += 2)
-        if (hinfo[k] != 0) throw Error(GMGS_ERR_NOT_SPD, "coarsest-level matrix is not positive definite");
-    for (size_t k = 1; k < hinfo.size(); k += 2)
-        if (hinfo[k] != 0) throw Error(GMGS_ERR_NOT_SPD, "coarsest-level factor is singular");
-    k_symmetrize_lower<<<blocks_for(c, (int64_t)n * n), 256, 0, c.stream>>>(n, M.kinv.as<double>());
+    CoarseBlocks& cb = M.cb;
+    cb = CoarseBlocks();
+    cb.n = n;
+    cb.B = coarse_block_order(n, bw);
+    cb.nb = (n + cb.B - 1) / cb.B;
+    const int64_t npad = (int64_t)cb.nb * cb.B;
+    const size_t blk_bytes = (size_t)cb.nb * cb.B * cb.B * sizeof(double);
+    if (blk_bytes > ((size_t)16 << 30))
+        throw Error(GMGS_ERR_RESOLUTION, "coarsest level too large for the block factorisation; use more levels");
+    cb.sinv = dalloc(blk_bytes);
+    cb.g = dalloc(blk_bytes);
+    GMGS_CUDA(cudaMemsetAsync(cb.sinv.p, 0, blk_bytes, c.stream));
+    GMGS_CUDA(cudaMemsetAsync(cb.g.p, 0, blk_bytes, c.stream));
+    k_assemble_blocks<<<blocks_for(c, (int64_t)n * 81), 256, 0, c.stream>>>(
+        lc.g, n, M.free_idx.as<int32_t>(), rank.as<int32_t>(), lc.emask.as<uint8_t>(), lc.etype.as<int32_t>(),
+        lc.Ks64.as<double>(), M.ke0_dev.as<double>(), lc.kscale, cb.B, cb.sinv.as<double>(), cb.g.as<double>());
     GMGS_LAUNCHED(c);
-    M.cvec_tmp = dalloc(nf * sizeof(double));
-    M.cvec_in = dalloc(nf * sizeof(double));
-    M.cvec_out = dalloc(nf * sizeof(double));
+    if (npad > n) {
+        k_pad_identity<<<(unsigned)((npad - n + 255) / 256), 256, 0, c.stream>>>(n, (int)npad, cb.B,
+                                                                               cb.sinv.as<double>());
+        GMGS_LAUNCHED(c);
+    }
+    c.trace_point("bc: coarsest free DOFs + block assembly");
+    factor_coarse(c, cb);
+    M.cvec_in = dalloc(npad * sizeof(double));
+    M.cvec_out = dalloc(npad * sizeof(double));
+    GMGS_CUDA(cudaMemsetAsync(M.cvec_in.p, 0, npad * sizeof(double), c.stream));
+    GMGS_CUDA(cudaMemsetAsync(M.cvec_out.p, 0, npad * sizeof(double), c.stream));
     GMGS_CUDA(cudaStreamSynchronize(c.stream));
-    c.trace_point("bc: symmetrise + vectors");
 }
 
 }  // namespace gmgs

@@ -30,7 +30,8 @@ struct Model {
     double normF = 0;
     // coarsest level
     int nfree = 0;
-    DevBuf free_idx, kinv, cvec_in, cvec_tmp, cvec_out;   // kinv: Linv (lower) | Linv^T (upper), row-major
+    DevBuf free_idx, cvec_in, cvec_out;   // free DOF slots; coarse vectors (cb.nb * cb.B long)
+    CoarseBlocks cb;
     // outer CG work vectors
     DevBuf cg_x, cg_r, cg_p, cg_dx, cg_q64, cg_y64, cg_z64;   // FP64 path
     DevBuf cg_q32, cg_y32, cg_z32, cg_r32;                     // mixed path

@@ -109,8 +109,7 @@ static void vcycle(Model& M, const T* r0, T* z) {
     }
     Level& lc = M.levels[L - 1];
     launch_gather<T>(c, M.nfree, M.free_idx.as<int32_t>(), lc.vr.as<T>(), M.cvec_in.as<double>());
-    launch_coarse_solve(c, M.nfree, M.kinv.as<double>(), M.cvec_in.as<double>(), M.cvec_tmp.as<double>(),
-                        M.cvec_out.as<double>());
+    launch_coarse_solve(c, M.cb, M.cvec_in.as<double>(), M.cvec_out.as<double>());
     launch_scatter<T>(c, M.nfree, M.free_idx.as<int32_t>(), M.cvec_out.as<double>(), lc.vx.as<T>());
     for (int l = L - 2; l >= 0; --l) {
         Level& lv = M.levels[l];
@@ -206,8 +205,7 @@ static void vcycle32(Model& M, const float* r32, float* z, bool with_dot, int do
     if (L == 2) c.mark(PK_COARSE, false);
     Level& lc = M.levels[L - 1];
     launch_gather<float>(c, M.nfree, M.free_idx.as<int32_t>(), lc.vr.as<float>(), M.cvec_in.as<double>());
-    launch_coarse_solve(c, M.nfree, M.kinv.as<double>(), M.cvec_in.as<double>(), M.cvec_tmp.as<double>(),
-                        M.cvec_out.as<double>());
+    launch_coarse_solve(c, M.cb, M.cvec_in.as<double>(), M.cvec_out.as<double>());
     launch_scatter<float>(c, M.nfree, M.free_idx.as<int32_t>(), M.cvec_out.as<double>(), lc.vx.as<float>());
     for (int l = L - 2; l >= 0; --l) {
         Level& lv = M.levels[l];

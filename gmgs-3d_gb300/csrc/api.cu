@@ -51,43 +51,84 @@ int guarded(gmgs_handle* h, F&& f) {
 
 void fail(int status, const char* msg) { throw gmgs::Error(status, msg); }
 
-// A freshly allocated host output buffer is backed by pages the OS maps and
-// zeroes on first write; a device-to-host copy into such a buffer runs at the
-// page-fault rate of one core (about 20-25 GB/s for GB-sized outputs on the
-// Grace host) instead of the link rate (about 190 GB/s).  HostPrefault writes
-// one byte per page of the output from a few host threads while the GPU is
-// still computing, so the copy that follows finds every page mapped.  The
-// buffer is an output: its contents are overwritten by the copy anyway.
+// Host buffers of a call: a copy between the device and pageable host memory
+// runs at link speed (about 190 GB/s on the Grace host) only when the pages
+// are already mapped and the driver takes its direct path; a freshly
+// allocated output is first faulted in page by page (20-30 GB/s on one core)
+// and large pageable copies were seen to drop to 5-8 GB/s at times.  Large
+// host ranges are therefore pinned for the duration of their copy
+// (cudaHostRegister, about 2 ms per GB once the pages exist) and unpinned
+// afterwards; a range that cannot be pinned (already pinned, or not
+// registrable) is copied pageable as before.
+constexpr size_t kPinMinBytes = 32u << 20;
+
+class HostPin {
+public:
+    HostPin(const void* p, size_t bytes, bool read_only) {
+        if (!p || bytes < kPinMinBytes) return;
+        unsigned flags = cudaHostRegisterPortable | (read_only ? cudaHostRegisterReadOnly : 0u);
+        if (cudaHostRegister(const_cast<void*>(p), bytes, flags) == cudaSuccess) p_ = const_cast<void*>(p);
+        else cudaGetLastError();
+    }
+    HostPin(const HostPin&) = delete;
+    HostPin& operator=(const HostPin&) = delete;
+    ~HostPin() {
+        if (p_ && cudaHostUnregister(p_) != cudaSuccess) cudaGetLastError();
+    }
+
+private:
+    void* p_ = nullptr;
+};
+
+// An output buffer is faulted in (one byte written per page, from up to 8
+// host threads) and then pinned while the GPU is still computing, so the
+// device-to-host copy that follows finds every page mapped and locked.  Its
+// contents are overwritten by the copy anyway.  join() before the copy; the
+// destructor unpins, so the object must outlive the copy's synchronisation.
 class HostPrefault {
 public:
     HostPrefault(void* p, size_t bytes) {
-        if (!p || bytes < kMinBytes) return;
-        const long pg = sysconf(_SC_PAGESIZE);
-        const size_t page = pg > 0 ? (size_t)pg : 4096;
-        const unsigned hc = std::thread::hardware_concurrency();
-        const size_t nt = std::min<size_t>(kMaxThreads, std::max<size_t>(1, hc / 2));
-        char* base = static_cast<char*>(p);
-        const size_t per = (bytes + nt - 1) / nt;
-        for (size_t t = 0; t < nt; ++t) {
-            const size_t b = t * per, e = std::min(bytes, b + per);
-            if (b >= e) break;
-            threads_.emplace_back([base, b, e, page]() {
-                volatile char* q = base;
-                for (size_t i = b; i < e; i += page) q[i] = 0;
-                q[e - 1] = 0;
-            });
-        }
+        if (!p || bytes < kPinMinBytes) return;
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return; }
+        manager_ = std::thread([this, p, bytes, dev]() {
+            const long pg = sysconf(_SC_PAGESIZE);
+            const size_t page = pg > 0 ? (size_t)pg : 4096;
+            const unsigned hc = std::thread::hardware_concurrency();
+            const size_t nt = std::min<size_t>(kMaxThreads, std::max<size_t>(1, hc / 2));
+            char* base = static_cast<char*>(p);
+            const size_t per = (bytes + nt - 1) / nt;
+            std::vector<std::thread> touch;
+            for (size_t t = 0; t < nt; ++t) {
+                const size_t b = t * per, e = std::min(bytes, b + per);
+                if (b >= e) break;
+                touch.emplace_back([base, b, e, page]() {
+                    volatile char* q = base;
+                    for (size_t i = b; i < e; i += page) q[i] = 0;
+                    q[e - 1] = 0;
+                });
+            }
+            for (auto& t : touch) t.join();
+            if (cudaSetDevice(dev) == cudaSuccess && cudaHostRegister(p, bytes, cudaHostRegisterPortable) == cudaSuccess)
+                pinned_ = p;
+            else
+                cudaGetLastError();
+        });
     }
+    HostPrefault(const HostPrefault&) = delete;
+    HostPrefault& operator=(const HostPrefault&) = delete;
     void join() {
-        for (auto& t : threads_) t.join();
-        threads_.clear();
+        if (manager_.joinable()) manager_.join();
     }
-    ~HostPrefault() { join(); }
+    ~HostPrefault() {
+        join();
+        if (pinned_ && cudaHostUnregister(pinned_) != cudaSuccess) cudaGetLastError();
+    }
 
 private:
-    static constexpr size_t kMinBytes = 32u << 20;
     static constexpr size_t kMaxThreads = 8;
-    std::vector<std::thread> threads_;
+    std::thread manager_;
+    void* pinned_ = nullptr;
 };
 
 // the reference's level rule (DiscretizeDesignDomain.m:29-41); returns numLevels
@@ -268,8 +309,10 @@ int gmgs_create(const int32_t* occ, int32_t ny, int32_t nx, int32_t nz, const do
         M.ctx.trace_point("create: start");
         {
             gmgs::DevBuf occ_dev = gmgs::dalloc((size_t)ny * nx * nz * sizeof(int32_t));
+            HostPin pin(occ, (size_t)ny * nx * nz * sizeof(int32_t), true);
             GMGS_CUDA(cudaMemcpyAsync(occ_dev.p, occ, (size_t)ny * nx * nz * sizeof(int32_t), cudaMemcpyHostToDevice,
                                       M.ctx.stream));
+            GMGS_CUDA(cudaStreamSynchronize(M.ctx.stream));
             M.ctx.trace_point("create: occupancy to device");
             gmgs::build_levels(M, occ_dev.as<int32_t>());
         }
@@ -306,7 +349,11 @@ int gmgs_set_density(gmgs_handle* h, const double* rho, double penal) {
         for (int64_t i = 0; i < ne; ++i)
             if (!(rho[i] > 0) || !std::isfinite(rho[i])) fail(GMGS_ERR_INVALID_ARGUMENT, "density must be positive");
         gmgs::DevBuf d = gmgs::dalloc(ne * sizeof(double));
-        GMGS_CUDA(cudaMemcpyAsync(d.p, rho, ne * sizeof(double), cudaMemcpyHostToDevice, M.ctx.stream));
+        {
+            HostPin pin(rho, ne * sizeof(double), true);
+            GMGS_CUDA(cudaMemcpyAsync(d.p, rho, ne * sizeof(double), cudaMemcpyHostToDevice, M.ctx.stream));
+            GMGS_CUDA(cudaStreamSynchronize(M.ctx.stream));
+        }
         M.penal = penal;
         gmgs::set_density_dev(M, d.as<double>());
         M.coarse_ready = false;
@@ -384,7 +431,9 @@ static int grad_impl(gmgs_handle* h, const double* ell_host, const double* ell_d
         const double* src = ell_dev;
         if (ell_host) {
             ec = gmgs::dalloc(3 * nn * sizeof(double));
+            HostPin pin(ell_host, 3 * nn * sizeof(double), true);
             GMGS_CUDA(cudaMemcpyAsync(ec.p, ell_host, 3 * nn * sizeof(double), cudaMemcpyHostToDevice, M.ctx.stream));
+            GMGS_CUDA(cudaStreamSynchronize(M.ctx.stream));
             src = ec.as<double>();
         }
         GMGS_CUDA(cudaMemsetAsync(ed.p, 0, 3 * S * sizeof(double), M.ctx.stream));
@@ -433,6 +482,7 @@ int gmgs_apply_operator(gmgs_handle* h, int32_t level, const double* x, double* 
         const int64_t nn = lv.n_node, S = lv.g.slots;
         gmgs::DevBuf xc = gmgs::dalloc(3 * nn * sizeof(double)), xd = gmgs::dalloc(3 * S * sizeof(double)),
                      yd = gmgs::dalloc(3 * S * sizeof(double));
+        HostPin pin_in(x, 3 * nn * sizeof(double), true), pin_out(y, 3 * nn * sizeof(double), false);
         GMGS_CUDA(cudaMemcpyAsync(xc.p, x, 3 * nn * sizeof(double), cudaMemcpyHostToDevice, M.ctx.stream));
         GMGS_CUDA(cudaMemsetAsync(xd.p, 0, 3 * S * sizeof(double), M.ctx.stream));
         gmgs::launch_compact_to_dense<double>(M.ctx, nn, S, lv.node_slot.as<int32_t>(), xc.as<double>(), xd.as<double>());
@@ -453,6 +503,7 @@ int gmgs_apply_preconditioner(gmgs_handle* h, const double* r, double* z) {
         const int64_t nn = lv.n_node, S = lv.g.slots;
         gmgs::DevBuf xc = gmgs::dalloc(3 * nn * sizeof(double)), xd = gmgs::dalloc(3 * S * sizeof(double)),
                      yd = gmgs::dalloc(3 * S * sizeof(double));
+        HostPin pin_in(r, 3 * nn * sizeof(double), true), pin_out(z, 3 * nn * sizeof(double), false);
         GMGS_CUDA(cudaMemcpyAsync(xc.p, r, 3 * nn * sizeof(double), cudaMemcpyHostToDevice, M.ctx.stream));
         GMGS_CUDA(cudaMemsetAsync(xd.p, 0, 3 * S * sizeof(double), M.ctx.stream));
         GMGS_CUDA(cudaMemsetAsync(yd.p, 0, 3 * S * sizeof(double), M.ctx.stream));

@@ -112,41 +112,46 @@ void gemm(Ctx& c, const Gemm& g, int m, int n, int k, double alpha, const double
 }
 
 // Cholesky of a 32 x 32 SPD tile (lower triangle of A, in place) and the
-// inverse of its factor into Li (zeros above the diagonal).  A pivot that is
-// not positive sets *info and is replaced by 1 so the arithmetic stays finite.
+// inverse of its factor into Li (zeros above the diagonal), one column per
+// step: the pivot's square root and reciprocal, column j of L, row j of L^-1
+// (forward substitution of L X = I carried along: X(j, c) is final once
+// scaled by 1/L(j,j)), then the rank-1 updates of the trailing part of A and
+// of the rows of X below j.  A pivot that is not positive sets *info and is
+// replaced by 1 so the arithmetic stays finite.
 __global__ void __launch_bounds__(256) k_chol_inv32(double* __restrict__ A, int lda, double* __restrict__ Li,
                                                     int ldl, int* __restrict__ info) {
-    __shared__ double a[32][33];   // a[c][r] = A(r, c)
-    __shared__ double x[32][33];   // x[c][r] = L^-1(r, c)
+    __shared__ double a[32][33];   // a[c][r] = A(r, c), becomes L
+    __shared__ double x[32][33];   // x[c][r] = X(r, c), becomes L^-1
+    __shared__ double dinv;
     const int t = threadIdx.x;
-    for (int e = t; e < 1024; e += 256) a[e >> 5][e & 31] = A[(int64_t)(e >> 5) * lda + (e & 31)];
+    for (int e = t; e < 1024; e += 256) {
+        const int cc = e >> 5, r = e & 31;
+        a[cc][r] = A[(int64_t)cc * lda + r];
+        x[cc][r] = r == cc ? 1.0 : 0.0;
+    }
     __syncthreads();
     for (int j = 0; j < 32; ++j) {
         if (t == 0) {
             const double d = a[j][j];
             const bool ok = d > 0.0 && d < INFINITY;
             if (!ok) atomicExch(info, 1);
-            a[j][j] = ok ? sqrt(d) : 1.0;
+            const double piv = ok ? sqrt(d) : 1.0;
+            a[j][j] = piv;
+            dinv = 1.0 / piv;
         }
         __syncthreads();
-        if (t > j && t < 32) a[j][t] /= a[j][j];
+        if (t > j && t < 32) a[j][t] *= dinv;                  // L(t, j)
+        if (t >= 32 && t - 32 <= j) x[t - 32][j] *= dinv;      // X(j, c), c <= j
         __syncthreads();
         for (int e = t; e < 1024; e += 256) {
             const int cc = e >> 5, r = e & 31;
-            if (cc > j && r >= cc) a[cc][r] = fma(-a[j][r], a[j][cc], a[cc][r]);
+            if (r > j) {
+                if (cc > j && r >= cc) a[cc][r] = fma(-a[j][r], a[j][cc], a[cc][r]);
+                if (cc <= j) x[cc][r] = fma(-a[j][r], x[cc][j], x[cc][r]);
+            }
         }
         __syncthreads();
     }
-    if (t < 32) {   // column t of L^-1 by forward substitution
-        for (int r = 0; r < t; ++r) x[t][r] = 0.0;
-        x[t][t] = 1.0 / a[t][t];
-        for (int r = t + 1; r < 32; ++r) {
-            double s = 0.0;
-            for (int m = t; m < r; ++m) s = fma(a[m][r], x[t][m], s);
-            x[t][r] = -s / a[r][r];
-        }
-    }
-    __syncthreads();
     for (int e = t; e < 1024; e += 256) {
         const int cc = e >> 5, r = e & 31;
         if (r >= cc) A[(int64_t)cc * lda + r] = a[cc][r];

@@ -189,10 +189,18 @@ class Solver:
             raise ValueError("rho must have one entry per solid voxel")
         self._check(self._lib.gmgs_set_density(self._h, _dptr(r), penal))
 
-    def solve(self, with_history=False):
-        """Return U (3*num_nodes, interleaved); raise on divergence."""
+    def solve(self, with_history=False, out=None):
+        """Return U (3*num_nodes, interleaved); raise on divergence.
+
+        out: optional float64 C-contiguous array of 3*num_nodes to write U into
+        (e.g. a pinned host buffer reused across solves); returned as U."""
         nn = self.num_nodes(1)
-        U = np.empty(3 * nn)
+        if out is None:
+            U = np.empty(3 * nn)
+        else:
+            U = out
+            if U.dtype != np.float64 or U.size != 3 * nn or not U.flags.c_contiguous or not U.flags.writeable:
+                raise ValueError("out must be a writeable C-contiguous float64 array of 3 * num_nodes")
         it = C.c_int32()
         rr = C.c_double()
         hist = np.zeros(3 * (self.params.max_it + 2)) if with_history else None

@@ -26,7 +26,18 @@ CASES = {
     "ragged_L3": (lambda: synthetic.sphere_voids(21, 13, 18, 6, 7), 3, 0.4),
     # five levels: level 4 stores one Galerkin matrix per element and is smoothed
     "block42_L5": (lambda: synthetic.make("block42_fp64")[0], 5, 0.4),
+    # a long column: the coarsest level (3 x 3 x 50 elements, 2376 free DOFs)
+    # splits into 19 diagonal blocks of order 128, so both sweeps of the
+    # two-ended block LDL^T run long chains
+    "column_L3": (lambda: synthetic.sphere_voids(9, 10, 200, 6, 5), 3, 0.4),
 }
+
+# V-cycle agreement bar.  The column's coarsest matrix has condition number
+# 2e7, so last-bit differences in the restricted residual (summation order of
+# the smoother and the restriction) come out of the coarsest solve amplified
+# to about cond * eps = 2e-9 relative; the dense cuSOLVER inverse factor used
+# before the block LDL^T gave 2.45e-9 here as well.
+VCYCLE_TOL = {"column_L3": 1e-8}
 
 
 def _pair(name, precision="fp64", tol=1e-3):
@@ -67,11 +78,11 @@ def test_operator_each_level(solved_pair):
 
 
 def test_vcycle(solved_pair):
-    _, o, s, _, _ = solved_pair
+    name, o, s, _, _ = solved_pair
     rng = np.random.default_rng(1)
     r = rng.standard_normal(o.levels[0].numDOFs)
     r[o.levels[0].fixedDOFs] = 0
-    assert rel(s.apply_preconditioner(r), o.vcycle(r)) < 1e-10
+    assert rel(s.apply_preconditioner(r), o.vcycle(r)) < VCYCLE_TOL.get(name, 1e-10)
 
 
 def test_pcg_history_and_displacement(solved_pair):

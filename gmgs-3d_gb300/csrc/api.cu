@@ -336,6 +336,9 @@ int gmgs_set_bc(gmgs_handle* h, const int32_t* fixed, int64_t nfixed, const doub
         h->fixed_host.assign(fixed, fixed + nfixed);
         h->loads_host.assign(loads, loads + 4 * nload);
         h->M.bc_set = true;
+        // the coarse fixed DOFs and the coarsest factorisation follow the new
+        // fixings at the next solve (SetupSolver.m:247-259)
+        h->M.coarse_ready = false;
         return GMGS_OK;
     });
 }
@@ -685,6 +688,7 @@ void gmgs_destroy(gmgs_handle* h) {
     if (!h) return;
     gmgs::Model& M = h->M;
     if (M.ctx.stream) cudaStreamSynchronize(M.ctx.stream);
+    gmgs::reset_graphs(M);
     M.levels.clear();
     for (auto& s : M.ctx.prof_slot)
         for (cudaEvent_t e : s.ev) cudaEventDestroy(e);

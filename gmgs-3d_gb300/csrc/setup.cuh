@@ -39,6 +39,12 @@ struct Model {
     Coef32 coef{};                                             // FP32 stencil + element matrix
     DevBuf scal;           // device scalars (see solver.cu)
     DevBuf dot_partials, dot_ticket;
+    // CUDA graphs of the mixed PCG iteration body (one per parity), valid for
+    // the solution buffer and the work-buffer generation they were captured with
+    cudaGraphExec_t cg_graph[2] = {nullptr, nullptr};
+    int64_t cg_graph_kernels[2] = {0, 0};
+    const double* cg_graph_x = nullptr;
+    uint64_t cg_graph_gen = 0, gen = 0;
     double* scal_host = nullptr;   // pinned
     int dot_blocks = 0;
     bool bc_set = false, coarse_ready = false, solved = false, ops_ready = false;
@@ -70,6 +76,7 @@ void set_density_dev(Model& M, const double* rho_dev);
 
 // solver.cu
 void alloc_work(Model& M);
+void reset_graphs(Model& M);   // destroy the captured PCG iteration graphs
 int pcg_solve(Model& M, const double* b_dense, double* x_dense, int32_t* iters, double* relres, double* hist);
 void vcycle_apply_fp64(Model& M, const double* r_dense, double* z_dense);
 void apply_operator_dense(Model& M, int level, const double* x_dense, double* y_dense);

@@ -141,3 +141,40 @@ def test_repeat_solve_is_bitwise_identical():
     u1 = s.solve()
     u2 = s.solve()
     assert np.array_equal(u1, u2)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_new_boundary_conditions_rebuild_the_coarse_levels(precision):
+    """A second set_bc on a solved handle (other fixings) solves exactly like a
+    fresh handle with those boundary conditions: the coarse fixed DOFs and the
+    coarsest factorisation are rebuilt."""
+    vox = synthetic.sphere_voids(21, 13, 18, 6, 7)
+    fixed_a, loads = synthetic.boundary_conditions(vox, 3)
+    s = Solver(vox, omega=0.4, num_levels=3, precision=precision)
+    s.set_bc(fixed_a, loads)
+    s.solve()
+    fixed_b = fixed_a[: len(fixed_a) // 2]          # half of the base plane
+    s.set_bc(fixed_b, loads)
+    u = s.solve()
+    f = Solver(vox, omega=0.4, num_levels=3, precision=precision)
+    f.set_bc(fixed_b, loads)
+    u_ref = f.solve()
+    assert s.iterations == f.iterations
+    assert np.array_equal(u, u_ref)
+
+
+def test_graph_replay_matches_eager_launches(monkeypatch):
+    """The mixed PCG iterations replayed from CUDA graphs (GMGS_GRAPH=1) give
+    bitwise the same solution as eager launches."""
+    vox = synthetic.make("block42_fp64")[0]
+    fixed, loads = synthetic.boundary_conditions(vox, 4)
+    s = Solver(vox, omega=0.4, num_levels=4, precision="mixed")
+    s.set_bc(fixed, loads)
+    monkeypatch.setenv("GMGS_GRAPH", "1")
+    u_graph = s.solve()
+    u_graph2 = s.solve()                            # cached graphs
+    monkeypatch.delenv("GMGS_GRAPH")
+    u_eager = s.solve()
+    assert s.iterations > 2
+    assert np.array_equal(u_graph, u_eager)
+    assert np.array_equal(u_graph2, u_eager)

@@ -440,20 +440,30 @@ __global__ void __launch_bounds__(256) k_perel_vdown(FineLevel L, const __grid_c
     const int n = nodes[warp];
     const uint32_t f = L.nflag[n];
     const int a = lane >> 3, j = lane & 7;      // lanes 24..31 idle (a == 3)
-    float part = 0.f;
+    // the element masks and matrix ids of all 8 elements first, so their
+    // loads are in flight together instead of one element after the other;
+    // void elements (etype 0) then contribute nothing, in the same order
+    uint32_t em = 0;
+    int t[8];
 #pragma unroll
     for (int e = 0; e < 8; ++e) {
-        const int A = e & 1, B = (e >> 1) & 1, C = e >> 2;
-        const int es = n - A - B * sx - C * sz;
-        if (!L.emask[es]) continue;                 // uniform across the warp
-        if (a < 3) {
+        const int es = n - (e & 1) - ((e >> 1) & 1) * sx - (e >> 2) * sz;
+        em |= L.emask[es] ? (1u << e) : 0u;
+        t[e] = L.etype ? L.etype[es] : 0;
+    }
+    float part = 0.f;
+    if (a < 3) {
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+            const int A = e & 1, B = (e >> 1) & 1, C = e >> 2;
+            if (!((em >> e) & 1u)) continue;        // uniform across the warp
+            const int es = n - A - B * sx - C * sz;
             const int ci = corner_of(A, B, C);
-            const int t = L.etype ? L.etype[es] : 0;
             const int nj = es + corner_y(j) + corner_x(j) * sx + corner_z(j) * sz;
             const float d0 = r[nj] * w[nj], d1 = r[nj + S] * w[nj + S], d2 = r[nj + 2 * S] * w[nj + 2 * S];
             const int off = (3 * ci + a) * 24 + 3 * j;
-            if (t > 0) {
-                const float* K = L.Ks + (int64_t)(t - 1) * KE + off;
+            if (t[e] > 0) {
+                const float* K = L.Ks + (int64_t)(t[e] - 1) * KE + off;
                 part = fmaf(K[0], d0, fmaf(K[1], d1, fmaf(K[2], d2, part)));
             } else {
                 const float k = L.kscale;

@@ -421,70 +421,67 @@ void launch_drop_last_dx(Ctx& c, int64_t n, double* x, const float* r32, const f
 
 // ---------------------------------------------------------------------------
 // V-cycle down-sweep at nodes that touch elements with their own Galerkin
-// matrix: one warp per node.  For each of the node's 8 elements the warp
-// reads the node's three rows of the element matrix (72 consecutive floats):
-// lane 8a + j takes row a, columns 3j..3j+2, i.e. the coupling of component a
-// to element node j, and multiplies it with node j's Jacobi step w r.  Each
-// lane keeps one row across the 8 elements; a shuffle reduction over the 8
-// lanes of a row sums it.  out = r - A (w r) with fixed rows zeroed (AtX.m:57).
+// matrix: eight lanes per node (four nodes per warp).  For each of the
+// node's 8 elements, lane j multiplies the node's three rows of the element
+// matrix at columns 3j..3j+2 (the coupling to element node j) with node j's
+// Jacobi step w r; each lane keeps the three row sums across the elements and
+// a shuffle reduction over the 8 lanes (xor 1, 2, 4) adds them up.  The
+// per-lane sums and the reduction order are those of a lane per (row,
+// column group), so the result does not depend on the lane layout.
+// out = r - A (w r) with fixed rows zeroed (AtX.m:57).
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_perel_vdown(FineLevel L, const __grid_constant__ Coef32 cf,
                                                      const int32_t* __restrict__ nodes, int count,
                                                      const float* __restrict__ r, const float* __restrict__ w,
                                                      float* __restrict__ out) {
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (warp >= count) return;
+    const int gl = blockIdx.x * blockDim.x + threadIdx.x;
+    const int node = gl >> 3, j = gl & 7;
+    const bool active = node < count;          // whole 8-lane groups; idle groups still shuffle
     const Grid& g = L.g;
     const int S = (int)g.slots, sx = g.py, sz = g.py * g.px;
-    const int n = nodes[warp];
-    const uint32_t f = L.nflag[n];
-    const int a = lane >> 3, j = lane & 7;      // lanes 24..31 idle (a == 3)
-    // the element masks and matrix ids of all 8 elements first, so their
-    // loads are in flight together instead of one element after the other;
-    // void elements (etype 0) then contribute nothing, in the same order
-    uint32_t em = 0;
-    int t[8];
-#pragma unroll
-    for (int e = 0; e < 8; ++e) {
-        const int es = n - (e & 1) - ((e >> 1) & 1) * sx - (e >> 2) * sz;
-        em |= L.emask[es] ? (1u << e) : 0u;
-        t[e] = L.etype ? L.etype[es] : 0;
-    }
-    float part = 0.f;
-    if (a < 3) {
+    const int n = active ? nodes[node] : 0;
+    float acc[3] = {0.f, 0.f, 0.f};
+    if (active) {
 #pragma unroll
         for (int e = 0; e < 8; ++e) {
             const int A = e & 1, B = (e >> 1) & 1, C = e >> 2;
-            if (!((em >> e) & 1u)) continue;        // uniform across the warp
             const int es = n - A - B * sx - C * sz;
+            if (!L.emask[es]) continue;         // uniform across the node's lanes
             const int ci = corner_of(A, B, C);
+            const int t = L.etype ? L.etype[es] : 0;
             const int nj = es + corner_y(j) + corner_x(j) * sx + corner_z(j) * sz;
             const float d0 = r[nj] * w[nj], d1 = r[nj + S] * w[nj + S], d2 = r[nj + 2 * S] * w[nj + 2 * S];
-            const int off = (3 * ci + a) * 24 + 3 * j;
-            if (t[e] > 0) {
-                const float* K = L.Ks + (int64_t)(t[e] - 1) * KE + off;
-                part = fmaf(K[0], d0, fmaf(K[1], d1, fmaf(K[2], d2, part)));
-            } else {
-                const float k = L.kscale;
-                part = fmaf(k * cf.K[off], d0, fmaf(k * cf.K[off + 1], d1, fmaf(k * cf.K[off + 2], d2, part)));
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                const int off = (3 * ci + a) * 24 + 3 * j;
+                if (t > 0) {
+                    const float* K = L.Ks + (int64_t)(t - 1) * KE + off;
+                    acc[a] = fmaf(K[0], d0, fmaf(K[1], d1, fmaf(K[2], d2, acc[a])));
+                } else {
+                    const float k = L.kscale;
+                    acc[a] = fmaf(k * cf.K[off], d0, fmaf(k * cf.K[off + 1], d1, fmaf(k * cf.K[off + 2], d2, acc[a])));
+                }
             }
         }
     }
-    part += __shfl_xor_sync(0xffffffffu, part, 1);
-    part += __shfl_xor_sync(0xffffffffu, part, 2);
-    part += __shfl_xor_sync(0xffffffffu, part, 4);
-    if (a < 3 && j == 0) {
-        const int i = n + a * S;
-        const float y = (f & (NF_FIX_X << a)) ? 0.f : part;
-        out[i] = r[i] - y;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        acc[a] += __shfl_xor_sync(0xffffffffu, acc[a], 1);
+        acc[a] += __shfl_xor_sync(0xffffffffu, acc[a], 2);
+        acc[a] += __shfl_xor_sync(0xffffffffu, acc[a], 4);
+    }
+    if (active && j < 3) {
+        const uint32_t f = L.nflag[n];
+        const float y = j == 0 ? acc[0] : (j == 1 ? acc[1] : acc[2]);
+        const int i = n + j * S;
+        out[i] = r[i] - ((f & (NF_FIX_X << j)) ? 0.f : y);
     }
 }
 
 void launch_perel_vdown(Ctx& c, const FineLevel& L, const Coef32& cf, const int32_t* nodes, int count, const float* r,
                         const float* w, float* out) {
     if (count <= 0) return;
-    const int blocks = (int)(((int64_t)count * 32 + 255) / 256);
+    const int blocks = (int)(((int64_t)count * 8 + 255) / 256);
     k_perel_vdown<<<blocks, 256, 0, c.stream>>>(L, cf, nodes, count, r, w, out);
     GMGS_LAUNCHED(c);
 }

@@ -796,6 +796,11 @@ void build_operators(Model& M) {
         }
     }
     c.trace_point("create: interior flags");
+    if (c.trace)
+        for (int l = 0; l < L; ++l)
+            std::fprintf(stderr, "[gmgs] level %d: %lld nodes, %lld elements, %lld own matrices, %lld nodes on them\n",
+                         l + 1, (long long)M.levels[l].n_node, (long long)M.levels[l].n_elem,
+                         (long long)M.levels[l].nK, (long long)M.levels[l].n_perel);
     M.ke0_dev = dalloc(KE * sizeof(double));
     GMGS_CUDA(cudaMemcpyAsync(M.ke0_dev.p, KeT, KE * sizeof(double), cudaMemcpyHostToDevice, c.stream));
     const double* ke0 = M.ke0_dev.as<double>();

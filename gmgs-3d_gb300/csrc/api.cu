@@ -156,8 +156,8 @@ void ensure_coarse(gmgs_handle* h) {
     if (!M.coarse_ready) {
         const auto t0 = Clock::now();
         M.ctx.trace_point("bc: start");
-        gmgs::build_coarse_bc(M);
-        gmgs::alloc_work(M);
+        // the work buffers are set up while the coarsest blocks factor
+        gmgs::build_coarse_bc(M, [&M]() { gmgs::alloc_work(M); });
         M.ctx.trace_point("bc: work buffers");
         M.coarse_ready = true;
         M.t_bc_ms = ms_since(t0);

@@ -327,7 +327,7 @@ int coarse_block_order(int n, int half_bandwidth) {
 
 int coarse_middle(int nb) { return (nb - 1) / 2; }
 
-void factor_coarse(Ctx& c, CoarseBlocks& cb) {
+void factor_coarse(Ctx& c, CoarseBlocks& cb, const std::function<void()>& overlap) {
     const int B = cb.B, nb = cb.nb, k = coarse_middle(nb);
     const int64_t B2 = (int64_t)B * B;
     double* D = cb.sinv.as<double>();   // A_ii on entry
@@ -390,6 +390,7 @@ void factor_coarse(Ctx& c, CoarseBlocks& cb) {
         if (k + 1 <= nb - 1)
             gemm(h, {Op::T, Op::N, 0, false}, B, B, B, 1.0, Eb(k + 1), B, Db(k + 1), B, 0.0, t2[1].as<double>(), B);
     }
+    if (overlap) overlap();
     for (int h = 0; h < 2; ++h) {
         GMGS_CUDA(cudaEventRecord(ev[1 + h], st[h]));
         GMGS_CUDA(cudaStreamWaitEvent(c.stream, ev[1 + h], 0));

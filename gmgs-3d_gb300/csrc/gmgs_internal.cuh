@@ -19,6 +19,7 @@
 #include <chrono>
 #include <cstdint>
 #include <cstdio>
+#include <functional>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -302,7 +303,9 @@ struct CoarseBlocks {
     DevBuf ticket;    // max(nb, 4) arrival counters (zero between launches)
 };
 int coarse_block_order(int n, int half_bandwidth);
-void factor_coarse(Ctx& c, CoarseBlocks& cb);
+// overlap: host work run while the two halves factor on their own streams
+// (it may enqueue on c.stream); may be empty
+void factor_coarse(Ctx& c, CoarseBlocks& cb, const std::function<void()>& overlap);
 // x = A^-1 r: r in cvec (overwritten), both nb*B long with zero padding
 void launch_coarse_solve(Ctx& c, const CoarseBlocks& cb, double* cvec, double* x);
 

@@ -9,7 +9,6 @@
 
 #include <algorithm>
 #include <cmath>
-#include <unordered_map>
 
 #include "setup.cuh"
 
@@ -516,13 +515,21 @@ __global__ void k_set_fixed(int64_t n, const int32_t* __restrict__ ids, const in
                             uint8_t* __restrict__ f) {
     GRID_STRIDE(i, n) f[node_slot[ids[i] - 1]] |= (NF_FIX_X | NF_FIX_Y | NF_FIX_Z);
 }
-__global__ void k_set_loads(int64_t n, const int32_t* __restrict__ ids, const double* __restrict__ fv,
+// loads rows (id, fx, fy, fz), 1-based compact node ids validated on the host;
+// the last row of each node wins (ApplyBoundaryCondition.m:9): its index is
+// the maximum over the node's rows
+__global__ void k_load_last(int64_t n, const double* __restrict__ loads, int32_t* __restrict__ last) {
+    GRID_STRIDE(i, n) atomicMax(last + ((int64_t)loads[4 * i] - 1), (int32_t)i);
+}
+__global__ void k_set_loads(int64_t n, const double* __restrict__ loads, const int32_t* __restrict__ last,
                             const int32_t* __restrict__ node_slot, int64_t S, double* __restrict__ F) {
     GRID_STRIDE(i, n) {
-        const int64_t s = node_slot[ids[i] - 1];
-        F[s] = fv[3 * i];
-        F[s + S] = fv[3 * i + 1];
-        F[s + 2 * S] = fv[3 * i + 2];
+        const int64_t id = (int64_t)loads[4 * i] - 1;
+        if (last[id] != (int32_t)i) continue;
+        const int64_t s = node_slot[id];
+        F[s] = loads[4 * i + 1];
+        F[s + S] = loads[4 * i + 2];
+        F[s + 2 * S] = loads[4 * i + 3];
     }
 }
 // coarse fixed DOFs: restricted indicator != 0 (SetupSolver.m:247-254)
@@ -923,36 +930,21 @@ void apply_bc(Model& M, const int32_t* fixed, int64_t nfixed, const double* load
     Ctx& c = M.ctx;
     Level& lv = M.levels[0];
     const int64_t nn = lv.n_node;
-    // host-side validation and "later duplicate wins" (ApplyBoundaryCondition.m:9)
-    std::vector<int32_t> fid(fixed, fixed + nfixed);
-    for (int32_t v : fid)
-        if (v < 1 || v > nn) throw Error(GMGS_ERR_INVALID_ARGUMENT, "fixed node id out of range");
-    std::unordered_map<int64_t, int64_t> last;
-    last.reserve((size_t)nload * 2);
+    for (int64_t i = 0; i < nfixed; ++i)
+        if (fixed[i] < 1 || fixed[i] > nn) throw Error(GMGS_ERR_INVALID_ARGUMENT, "fixed node id out of range");
     for (int64_t i = 0; i < nload; ++i) {
         const double idd = loads[4 * i];
         if (!(idd >= 1 && idd <= (double)nn) || idd != std::floor(idd))
             throw Error(GMGS_ERR_INVALID_ARGUMENT, "load node id out of range");
         for (int k = 1; k < 4; ++k)
             if (!std::isfinite(loads[4 * i + k])) throw Error(GMGS_ERR_NONFINITE, "non-finite load");
-        last[(int64_t)idd] = i;
-    }
-    std::vector<int32_t> lid;
-    std::vector<double> lval;
-    lid.reserve(last.size());
-    lval.reserve(3 * last.size());
-    for (int64_t i = 0; i < nload; ++i) {
-        const int64_t id = (int64_t)loads[4 * i];
-        if (last[id] != i) continue;
-        lid.push_back((int32_t)id);
-        for (int k = 1; k < 4; ++k) lval.push_back(loads[4 * i + k]);
     }
     DevBuf dfix = dalloc(std::max<int64_t>(1, nfixed) * sizeof(int32_t));
-    DevBuf dlid = dalloc(std::max<size_t>(1, lid.size()) * sizeof(int32_t));
-    DevBuf dlv = dalloc(std::max<size_t>(1, lval.size()) * sizeof(double));
-    GMGS_CUDA(cudaMemcpyAsync(dfix.p, fid.data(), nfixed * sizeof(int32_t), cudaMemcpyHostToDevice, c.stream));
-    GMGS_CUDA(cudaMemcpyAsync(dlid.p, lid.data(), lid.size() * sizeof(int32_t), cudaMemcpyHostToDevice, c.stream));
-    GMGS_CUDA(cudaMemcpyAsync(dlv.p, lval.data(), lval.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    DevBuf dld = dalloc(std::max<int64_t>(1, nload) * 4 * sizeof(double));
+    DevBuf last = dalloc(std::max<int64_t>(1, nn) * sizeof(int32_t));
+    GMGS_CUDA(cudaMemcpyAsync(dfix.p, fixed, nfixed * sizeof(int32_t), cudaMemcpyHostToDevice, c.stream));
+    GMGS_CUDA(cudaMemcpyAsync(dld.p, loads, nload * 4 * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    GMGS_CUDA(cudaMemsetAsync(last.p, 0xff, std::max<int64_t>(1, nn) * sizeof(int32_t), c.stream));   // -1
     k_clear_fixed<<<blocks_for(c, lv.g.slots), 256, 0, c.stream>>>(lv.g.slots, lv.nflag.as<uint8_t>());
     GMGS_LAUNCHED(c);
     k_set_fixed<<<blocks_for(c, nfixed), 256, 0, c.stream>>>(nfixed, dfix.as<int32_t>(), lv.node_slot.as<int32_t>(),
@@ -960,14 +952,15 @@ void apply_bc(Model& M, const int32_t* fixed, int64_t nfixed, const double* load
     GMGS_LAUNCHED(c);
     if (!M.F.p) M.F = dalloc(3 * lv.g.slots * sizeof(double));
     GMGS_CUDA(cudaMemsetAsync(M.F.p, 0, 3 * lv.g.slots * sizeof(double), c.stream));
-    k_set_loads<<<blocks_for(c, (int64_t)lid.size()), 256, 0, c.stream>>>(
-        (int64_t)lid.size(), dlid.as<int32_t>(), dlv.as<double>(), lv.node_slot.as<int32_t>(), lv.g.slots,
-        M.F.as<double>());
+    k_load_last<<<blocks_for(c, nload), 256, 0, c.stream>>>(nload, dld.as<double>(), last.as<int32_t>());
+    GMGS_LAUNCHED(c);
+    k_set_loads<<<blocks_for(c, nload), 256, 0, c.stream>>>(nload, dld.as<double>(), last.as<int32_t>(),
+                                                            lv.node_slot.as<int32_t>(), lv.g.slots, M.F.as<double>());
     GMGS_LAUNCHED(c);
     GMGS_CUDA(cudaStreamSynchronize(c.stream));
 }
 
-void build_coarse_bc(Model& M) {
+void build_coarse_bc(Model& M, const std::function<void()>& overlap) {
     Ctx& c = M.ctx;
     const int L = M.num_levels;
     // restricted fixed indicator, level by level (SetupSolver.m:247-254)
@@ -1044,7 +1037,7 @@ void build_coarse_bc(Model& M) {
         GMGS_LAUNCHED(c);
     }
     c.trace_point("bc: coarsest free DOFs + block assembly");
-    factor_coarse(c, cb);
+    factor_coarse(c, cb, overlap);
     M.cvec_in = dalloc(npad * sizeof(double));
     M.cvec_out = dalloc(npad * sizeof(double));
     GMGS_CUDA(cudaMemsetAsync(M.cvec_in.p, 0, npad * sizeof(double), c.stream));

@@ -71,7 +71,8 @@ void stress_coefficients(double E, double nu, const double ele[3], double c[6]);
 void build_levels(Model& M, const int32_t* occ_dev);
 void build_operators(Model& M);
 void apply_bc(Model& M, const int32_t* fixed, int64_t nfixed, const double* loads, int64_t nload);
-void build_coarse_bc(Model& M);
+// overlap: see factor_coarse
+void build_coarse_bc(Model& M, const std::function<void()>& overlap = {});
 void set_density_dev(Model& M, const double* rho_dev);
 
 // solver.cu

@@ -178,3 +178,23 @@ def test_graph_replay_matches_eager_launches(monkeypatch):
     assert s.iterations > 2
     assert np.array_equal(u_graph, u_eager)
     assert np.array_equal(u_graph2, u_eager)
+
+
+def test_duplicate_load_rows_last_one_wins():
+    """ApplyBoundaryCondition.m:9: a node listed twice in the loading
+    condition takes its later row (the device picks the largest row index)."""
+    vox = synthetic.sphere_voids(21, 13, 18, 6, 7)
+    fixed, loads = synthetic.boundary_conditions(vox, 3)
+    loads = np.asarray(loads, dtype=np.float64).reshape(-1, 4)
+    early = loads[:5].copy()
+    early[:, 1:] = 7.0                                   # overridden by the rows that follow
+    late = loads[-3:].copy()
+    late[:, 1:] *= 2.0                                   # overrides the rows before
+    dup = np.vstack([early, loads, late])
+    expect = loads.copy()
+    expect[-3:, 1:] *= 2.0
+    a = Solver(vox, omega=0.4, num_levels=3)
+    a.set_bc(fixed, dup)
+    b = Solver(vox, omega=0.4, num_levels=3)
+    b.set_bc(fixed, expect)
+    assert np.array_equal(a.solve(), b.solve())

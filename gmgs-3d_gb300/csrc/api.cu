@@ -336,9 +336,9 @@ int gmgs_set_bc(gmgs_handle* h, const int32_t* fixed, int64_t nfixed, const doub
         h->fixed_host.assign(fixed, fixed + nfixed);
         h->loads_host.assign(loads, loads + 4 * nload);
         h->M.bc_set = true;
-        // the coarse fixed DOFs and the coarsest factorisation follow the new
-        // fixings at the next solve (SetupSolver.m:247-259)
-        h->M.coarse_ready = false;
+        // like the reference, a later call changes level 1 only: the coarse
+        // fixed DOFs and the coarsest factorisation come from SetupSolver(),
+        // which GetDeformation.m:12-16 runs once per hierarchy
         return GMGS_OK;
     });
 }

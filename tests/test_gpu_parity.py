@@ -143,24 +143,26 @@ def test_repeat_solve_is_bitwise_identical():
     assert np.array_equal(u1, u2)
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_new_boundary_conditions_rebuild_the_coarse_levels(precision):
-    """A second set_bc on a solved handle (other fixings) solves exactly like a
-    fresh handle with those boundary conditions: the coarse fixed DOFs and the
-    coarsest factorisation are rebuilt."""
+def test_second_boundary_condition_changes_level_one_only():
+    """GetDeformation.m:12-16 runs SetupSolver() once: new fixings given to a
+    solved model change the finest level, while the coarse fixed DOFs and the
+    coarsest factorisation keep the first ones.  The GPU and the oracle
+    follow the same call sequence to the same iterations and displacement."""
     vox = synthetic.sphere_voids(21, 13, 18, 6, 7)
     fixed_a, loads = synthetic.boundary_conditions(vox, 3)
-    s = Solver(vox, omega=0.4, num_levels=3, precision=precision)
+    fixed_b = fixed_a[: len(fixed_a) // 2]          # half of the base plane
+    o = Oracle(vox, Params(omega=0.4, num_levels=3))
+    o.apply_boundary_condition(fixed_a, loads)
+    o.get_deformation()
+    o.apply_boundary_condition(fixed_b, loads)
+    u_ref = o.get_deformation()
+    s = Solver(vox, omega=0.4, num_levels=3)
     s.set_bc(fixed_a, loads)
     s.solve()
-    fixed_b = fixed_a[: len(fixed_a) // 2]          # half of the base plane
     s.set_bc(fixed_b, loads)
     u = s.solve()
-    f = Solver(vox, omega=0.4, num_levels=3, precision=precision)
-    f.set_bc(fixed_b, loads)
-    u_ref = f.solve()
-    assert s.iterations == f.iterations
-    assert np.array_equal(u, u_ref)
+    assert s.iterations == o.iterations
+    assert rel(u, u_ref) < 1e-6
 
 
 def test_graph_replay_matches_eager_launches(monkeypatch):

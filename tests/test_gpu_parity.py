@@ -200,3 +200,18 @@ def test_duplicate_load_rows_last_one_wins():
     b = Solver(vox, omega=0.4, num_levels=3)
     b.set_bc(fixed, expect)
     assert np.array_equal(a.solve(), b.solve())
+
+
+def test_solve_into_caller_buffer():
+    """Solver.solve(out=...) writes U into the caller's array (the bench keeps
+    it in pinned host memory) with the same values as a fresh output."""
+    o, s = _pair("ragged_L3")
+    u = s.solve()
+    buf = np.full_like(u, np.nan)
+    u2 = s.solve(out=buf)
+    assert u2 is buf
+    assert np.array_equal(buf, u)
+    with pytest.raises(ValueError):
+        s.solve(out=np.zeros(u.size, dtype=np.float32))
+    with pytest.raises(ValueError):
+        s.solve(out=np.zeros(u.size + 3))

@@ -111,10 +111,12 @@ __device__ __forceinline__ void epi_fetch(const FineArgs& a, int S, int n, EpiDa
     }
 }
 
-// 64 registers (4 CTAs per SM) for the stencil-only modes; the CG update
+// 48 registers (5 CTAs per SM) for the stencil-only modes; the CG update
 // holds FP64 state and keeps 80 registers (3 CTAs) without spilling.
+// Measured on the 153M-DOF model: 5 CTAs/SM took the down-sweep from 1.16 to
+// 1.13 ms and the direction kernel from 1.26 to 1.22 ms against 4 CTAs/SM.
 template <int MODE>
-__global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? 3 : 4)
+__global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? 3 : 5)
     k_fine(FineLevel L, const __grid_constant__ Coef32 cf, FineArgs a, int zc) {
     __shared__ float ring[RING][3 * PLANE];
     __shared__ double sh[32];
@@ -249,7 +251,10 @@ __global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? 3 : 4)
 
 static int pick_zc(const Grid& g, const Ctx& c) {
     const int64_t cols = (int64_t)((g.ny + 1 + TY - 1) / TY) * ((g.nx + 1 + TX - 1) / TX);
-    const int64_t want = (int64_t)c.num_sms * 3 * 12;     // ~12 waves of resident CTAs
+    // ~24 waves of 3 resident CTAs: shorter z-chunks balance the tail and let
+    // empty column tiles of real geometry skip more (12 waves: 214 -> 208 ms
+    // on the 153M-DOF block, 286 -> 271 ms on kitten 512; 48 waves: slower)
+    const int64_t want = (int64_t)c.num_sms * 3 * 24;
     int64_t zc = (cols * (g.nz + 1) + want - 1) / want;
     if (zc < 4) zc = 4;
     if (zc > 64) zc = 64;

@@ -45,7 +45,7 @@ enum gmgs_status {
     GMGS_ERR_MAX_ITERATIONS = 7,    /* CG_solver.m:52-55 (a warning there; U is still returned) */
     GMGS_ERR_NONFINITE = 8,         /* NaN/Inf residual */
     GMGS_ERR_NO_SOLUTION = 9,       /* stress/gradient before a solve: GetCartesianStress.m:7-9 */
-    GMGS_ERR_CUDA = 10,             /* CUDA runtime or cuSOLVER failure */
+    GMGS_ERR_CUDA = 10,             /* CUDA runtime failure */
     GMGS_ERR_OUT_OF_MEMORY = 11,
     GMGS_ERR_STATE = 12,            /* call order (e.g. solve before set_bc) */
     GMGS_ERR_MESH = 13              /* a mesh the reference's voxeliser cannot handle (Voxelize.m:176-203) */

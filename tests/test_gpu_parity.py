@@ -35,8 +35,8 @@ CASES = {
 # V-cycle agreement bar.  The column's coarsest matrix has condition number
 # 2e7, so last-bit differences in the restricted residual (summation order of
 # the smoother and the restriction) come out of the coarsest solve amplified
-# to about cond * eps = 2e-9 relative; the dense cuSOLVER inverse factor used
-# before the block LDL^T gave 2.45e-9 here as well.
+# to about cond * eps = 2e-9 relative; a dense inverse Cholesky factor of the
+# whole coarsest matrix gives 2.45e-9 here as well.
 VCYCLE_TOL = {"column_L3": 1e-8}
 
 

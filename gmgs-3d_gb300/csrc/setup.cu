@@ -352,6 +352,31 @@ __global__ void k_etype(int64_t n, const uint8_t* __restrict__ emask, const int3
     }
 }
 
+// Level 2 with a uniform finest material (SetupSolver.m:39-68): a "unique"
+// element's Galerkin matrix is the sum of P_j^T Ke0 P_j over its solid
+// children, so it is fixed by the 8-bit child-occupancy pattern.  One matrix
+// per pattern present replaces one per element: pat[s] = pattern (0 for
+// void and all-solid elements), rep[p] = the lowest slot with pattern p.
+__global__ void k_child_pattern(Grid gc, Grid gf, const uint8_t* __restrict__ emf, const int32_t* __restrict__ needK,
+                                int32_t* __restrict__ pat, int32_t* __restrict__ rep) {
+    GRID_STRIDE(s, gc.slots) {
+        int32_t p = 0;
+        if (needK[s]) {
+            int iy, ix, iz;
+            slot_coords(gc, s, iy, ix, iz);
+            for (int j = 0; j < 8; ++j)
+                if (emf[gf.slot(2 * iy + (j & 1), 2 * ix + ((j >> 1) & 1), 2 * iz + (j >> 2))]) p |= 1 << j;
+            atomicMin(rep + p, (int32_t)s);
+        }
+        pat[s] = p;
+    }
+}
+// etype = 1 + the rank of the element's pattern among the patterns present
+__global__ void k_etype_pattern(int64_t n, const uint8_t* __restrict__ emask, const int32_t* __restrict__ pat,
+                                const int32_t* __restrict__ rank, int32_t* __restrict__ etype) {
+    GRID_STRIDE(i, n) etype[i] = emask[i] ? (pat[i] ? rank[pat[i]] + 1 : 0) : -1;
+}
+
 // ---------------------------------------------------------------------------
 // Galerkin coarse element matrices: Ks_c = sum_j P_j^T K_j P_j over solid
 // children j (SetupSolver.m:36-196 with the 81x24 trilinear table).
@@ -704,6 +729,38 @@ void build_levels(Model& M, const int32_t* occ_dev) {
                                                                     fv.etype.as<int32_t>(), kmode,
                                                                     lv.emask.as<uint8_t>(), need.as<int32_t>());
         GMGS_LAUNCHED(c);
+        if (kmode == 1) {
+            // one Galerkin matrix per child-occupancy pattern present (at most 254)
+            DevBuf rep = dalloc(256 * sizeof(int32_t));
+            GMGS_CUDA(cudaMemsetAsync(rep.p, 0x7f, 256 * sizeof(int32_t), c.stream));   // > any slot
+            k_child_pattern<<<blocks_for(c, lv.g.slots), 256, 0, c.stream>>>(
+                lv.g, fv.g, fv.emask.as<uint8_t>(), need.as<int32_t>(), need0.as<int32_t>(), rep.as<int32_t>());
+            GMGS_LAUNCHED(c);
+            int32_t hrep[256];
+            GMGS_CUDA(cudaMemcpyAsync(hrep, rep.p, sizeof(hrep), cudaMemcpyDeviceToHost, c.stream));
+            GMGS_CUDA(cudaStreamSynchronize(c.stream));
+            int32_t hrank[256], hslot[256];
+            int nk = 0;
+            for (int p = 0; p < 256; ++p) {
+                hrank[p] = -1;
+                if (p > 0 && hrep[p] != 0x7f7f7f7f) {
+                    hrank[p] = nk;
+                    hslot[nk++] = hrep[p];
+                }
+            }
+            lv.nK = nk;
+            lv.etype = dalloc(lv.g.slots * sizeof(int32_t));
+            lv.kslot = dalloc(std::max(1, nk) * sizeof(int32_t));
+            DevBuf drank = dalloc(256 * sizeof(int32_t));
+            GMGS_CUDA(cudaMemcpyAsync(drank.p, hrank, sizeof(hrank), cudaMemcpyHostToDevice, c.stream));
+            if (nk > 0)
+                GMGS_CUDA(cudaMemcpyAsync(lv.kslot.p, hslot, nk * sizeof(int32_t), cudaMemcpyHostToDevice, c.stream));
+            k_etype_pattern<<<blocks_for(c, lv.g.slots), 256, 0, c.stream>>>(
+                lv.g.slots, lv.emask.as<uint8_t>(), need0.as<int32_t>(), drank.as<int32_t>(), lv.etype.as<int32_t>());
+            GMGS_LAUNCHED(c);
+            GMGS_CUDA(cudaStreamSynchronize(c.stream));
+            continue;
+        }
         GMGS_CUDA(cudaMemcpyAsync(need0.p, need.p, lv.g.slots * sizeof(int32_t), cudaMemcpyDeviceToDevice, c.stream));
         lv.nK = exclusive_scan(c, need.as<int32_t>(), lv.g.slots);
         lv.etype = dalloc(lv.g.slots * sizeof(int32_t));

@@ -216,3 +216,27 @@ def test_only_value_one_is_solid():
     vox[0, 0, 0] = 2
     lv, L, _ = G.discretize(vox, G.Params(num_levels=2))
     assert lv.numElements == 63
+
+
+def test_level2_galerkin_matrix_is_fixed_by_the_child_pattern():
+    """SetupSolver.m:39-68 with a uniform finest material: a unique level-2
+    element's Galerkin matrix depends only on which of its 8 children are
+    solid.  The device keeps one matrix per pattern present on that basis."""
+    from gmgs import synthetic
+    vox = synthetic.sphere_voids(21, 13, 18, 6, 7)
+    o = G.Oracle(vox, G.Params(num_levels=3))
+    o.setup()
+    lv = o.levels[1]
+    assert lv.storingState == 2 and len(lv.uniqueElements) > 20
+    masks = (lv.elementUpwardMap[lv.uniqueElements] != 0) @ (1 << np.arange(8))
+    by_mask = {}
+    for k, m in enumerate(masks):
+        by_mask.setdefault(int(m), []).append(lv.Ks[1 + k])
+    assert len(by_mask) < len(masks)
+    for mats in by_mask.values():
+        for K in mats[1:]:
+            assert np.array_equal(K, mats[0])
+    firsts = [m[0] for m in by_mask.values()]
+    for i in range(len(firsts)):
+        for j in range(i + 1, len(firsts)):
+            assert not np.allclose(firsts[i], firsts[j])

@@ -40,8 +40,14 @@ def flags(debug: bool) -> list[str]:
     return ARCH + f
 
 
+def obj_dir(debug: bool) -> Path:
+    """Object files of each build mode live apart, so a debug build never
+    leaves objects that a later release build would take as up to date."""
+    return BUILD / ("debug" if debug else "release")
+
+
 def compile_one(src: str, debug: bool) -> Path:
-    out = BUILD / (Path(src).stem + ".o")
+    out = obj_dir(debug) / (Path(src).stem + ".o")
     srcp = CSRC / src
     deps = [srcp] + list(CSRC.glob("*.cuh")) + [ROOT / "include" / "gmgs.h"]
     if out.exists() and all(out.stat().st_mtime >= d.stat().st_mtime for d in deps) and not debug:
@@ -56,17 +62,21 @@ def compile_one(src: str, debug: bool) -> Path:
 
 
 def build(debug: bool = False, jobs: int | None = None) -> Path:
-    BUILD.mkdir(parents=True, exist_ok=True)
+    obj_dir(debug).mkdir(parents=True, exist_ok=True)
     srcs = [s for s in SOURCES if (CSRC / s).exists()]
     with cf.ThreadPoolExecutor(max_workers=jobs or min(8, len(srcs))) as ex:
         objs = list(ex.map(lambda s: compile_one(s, debug), srcs))
     newest = max(o.stat().st_mtime for o in objs)
-    if LIB.exists() and LIB.stat().st_mtime >= newest and not debug:
+    mode = "debug" if debug else "release"
+    stamp = BUILD / "libgmgs.mode"      # the mode the in-tree library was last linked in
+    if (LIB.exists() and LIB.stat().st_mtime >= newest and not debug and stamp.exists()
+            and stamp.read_text() == mode):
         return LIB
     cmd = [nvcc(), *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcudart"]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
+    stamp.write_text(mode)
     return LIB
 
 

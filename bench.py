@@ -65,7 +65,11 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison solve")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle sample")
-    ap.add_argument("--cpu-scale", type=float, default=0.125)
+    ap.add_argument("--cpu-scale", type=float, default=0.25,
+                    help="linear scale of the reduced model the CPU oracle is timed on")
+    ap.add_argument("--cpu-threads", type=int, default=0, help="BLAS/OpenMP threads of the CPU oracle (0: all cores)")
+    ap.add_argument("--no-cpu-config1", action="store_true",
+                    help="skip the measured CPU solve of the 42 x 37 x 64 workload")
     # a real mesh instead of the synthetic workload: the reference's demo inputs
     # (data/<model>.ply, data/demo_BC_<model>_<res>_fixedNodes.dat / _loadingVec.dat)
     ap.add_argument("--mesh", default=None, help="ASCII .ply triangle mesh (CreateVoxilizedModel input)")
@@ -125,47 +129,93 @@ class ClockSampler:
 
 
 # --------------------------------------------------------------------------
-# CPU oracle sample (the reference's algorithm restated in NumPy), in a child process
+# CPU oracle (the reference's algorithm restated in NumPy) in a child process
 # --------------------------------------------------------------------------
-CPU_SAMPLE = r"""
+# Two modes.  "iters": set up a reduced model of the workload once (timed, with
+# the coarsest factorisation timed on its own), then time `n` single PCG
+# iterations from x = 0 (CG_solver.m's loop body: Jacobi step, V-cycle, K p,
+# the vector updates).  "full": set up and solve a workload to tolerance and
+# save U for the GPU comparison.  The child's BLAS and OpenMP thread counts are
+# set from the parent (--cpu-threads, default every host core) and reported.
+CPU_WORKER = r"""
 import json, os, sys, time
+cfg = json.loads(sys.argv[2])
 sys.path[:0] = [sys.argv[1] + '/gmgs-3d_gb300', sys.argv[1] + '/oracle']
 import numpy as np
 from gmgs import synthetic
 from gmgs_oracle import Oracle, Params
-w = synthetic.WORKLOADS[sys.argv[2]]
-scale = float(sys.argv[3]); omega = float(sys.argv[4]); iters = int(sys.argv[5])
-drop = max(0, int(round(-np.log2(scale))))
-L = max(2, (w.num_levels or 5) - drop)
-vox = synthetic.sphere_voids(max(2, round(w.nelx*scale)), max(2, round(w.nely*scale)), max(2, round(w.nelz*scale)), max(1, round(w.voids*scale**2)), w.seed)
+w = synthetic.WORKLOADS[cfg["workload"]]
+scale = cfg["scale"]
+nelx, nely, nelz = (max(2, int(round(n * scale))) for n in (w.nelx, w.nely, w.nelz))
+if scale == 1.0:
+    voids, L = w.voids, synthetic.level_count(nely, nelx, nelz, w.num_levels)
+else:
+    # the void volume fraction is kept; dropping one level per halving keeps
+    # the coarsest level (and its dense factorisation) the size of the full model's
+    voids = max(1, round(w.voids * scale ** 3))
+    L = max(2, synthetic.level_count(w.nely, w.nelx, w.nelz, w.num_levels) - int(round(-np.log2(scale))))
+vox = synthetic.sphere_voids(nelx, nely, nelz, voids, w.seed)
 fixed, loads = synthetic.boundary_conditions(vox, L)
 t0 = time.perf_counter()
-o = Oracle(vox, Params(omega=omega, num_levels=L, max_it=iters - 1))
+o = Oracle(vox, Params(omega=cfg["omega"], num_levels=L, tol=w.tol))
 o.apply_boundary_condition(fixed, loads)
-if w.rho_range is not None:
+if w.rho_range is not None and cfg.get("density", True):
     o.set_density(synthetic.density(int(vox.sum()), w.rho_range, w.seed), w.penal)
+t_fact = [0.0]
+_fact = o._factorize_coarsest
+def _timed_fact():
+    t = time.perf_counter(); _fact(); t_fact[0] += time.perf_counter() - t
+o._factorize_coarsest = _timed_fact
 o.setup()
 t1 = time.perf_counter()
-with np.errstate(all='ignore'):
-    o.cg(o.F)
-t2 = time.perf_counter()
-print(json.dumps({"dofs": int(o.levels[0].numDOFs), "setup_s": t1 - t0, "iter_s": (t2 - t1) / o.iterations,
-                  "its": o.iterations, "shape": list(vox.shape), "levels": L}))
+out = {"dofs": int(o.levels[0].numDOFs), "setup_s": t1 - t0, "coarsest_factor_s": t_fact[0],
+       "shape": list(vox.shape), "voids": voids, "levels": L,
+       "threads": {k: os.environ.get(k) for k in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")}}
+try:
+    from threadpoolctl import threadpool_info
+    out["blas_threads"] = [i.get("num_threads") for i in threadpool_info() if i.get("user_api") == "blas"]
+except ImportError:
+    pass
+if cfg["mode"] == "iters":
+    times = []
+    with np.errstate(all='ignore'):
+        for _ in range(cfg["n"]):
+            t = time.perf_counter()
+            o.cg(o.F, max_it=0)              # one iteration of the loop from x = 0
+            times.append(time.perf_counter() - t)
+    out["iter_times_s"] = times
+else:
+    u = o.get_deformation()
+    t2 = time.perf_counter()
+    out.update({"solve_s": t2 - t1, "iterations": int(o.iterations), "relres": float(o.relres)})
+    np.save(cfg["u_path"], u)
+print(json.dumps(out))
 """
 
 
-def cpu_sample(workload: str, scale: float, omega: float, iters: int = 8) -> dict:
-    res = subprocess.run([sys.executable, "-c", CPU_SAMPLE, str(ROOT), workload, str(scale), str(omega), str(iters)],
-                         capture_output=True, text=True, timeout=900)
+def cpu_threads(a) -> int:
+    return a.cpu_threads or os.cpu_count() or 1
+
+
+def cpu_worker(cfg: dict, threads: int, timeout: float = 1200) -> dict:
+    env = dict(os.environ)
+    for k in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+        env[k] = str(threads)
+    res = subprocess.run([sys.executable, "-c", CPU_WORKER, str(ROOT), json.dumps(cfg)], capture_output=True,
+                         text=True, timeout=timeout, env=env)
     if res.returncode != 0:
         raise RuntimeError(res.stderr[-2000:])
     return json.loads(res.stdout.strip().splitlines()[-1])
 
 
-def cpu_extrapolate(sample: dict, dofs_full: int, its_full: int) -> float:
-    """Seconds for the full solve, scaled linearly in DOFs from the sample."""
+def cpu_extrapolate(sample: dict, iter_s: float, dofs_full: int, its_full: int) -> float:
+    """Seconds for the full solve from a reduced-model sample: the per-iteration
+    time and the setup without the coarsest factorisation scale with the DOF
+    count; the coarsest factorisation is the same size in the sample (one level
+    fewer per halving) and is counted once."""
     ratio = dofs_full / sample["dofs"]
-    return (sample["setup_s"] + sample["iter_s"] * its_full) * ratio
+    setup = (sample["setup_s"] - sample["coarsest_factor_s"]) * ratio + sample["coarsest_factor_s"]
+    return setup + iter_s * its_full * ratio
 
 
 # --------------------------------------------------------------------------
@@ -188,6 +238,13 @@ def dist_env():
 
 
 def run_reference(a):
+    """The reference's CPU path (the NumPy oracle port; MATLAB cannot run
+    here) on the host cores.  The full workload would take about two hours on
+    the CPU, so every step is one measured PCG iteration of a reduced model of
+    the same generator (a quarter of the resolution, two levels fewer: the same
+    coarsest level), set up once beforehand.  `value` is the full solve
+    extrapolated from those measurements and is labelled as such; the measured
+    figures are reported beside it."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
@@ -201,24 +258,29 @@ def run_reference(a):
     p[:nely, :nelx, :nelz] = vox
     dofs_full = 3 * int(synthetic.solid_node_mask(p).sum())
     its_full = int(os.environ.get("GMGS_REF_ITERS", "0")) or REF_ITERATIONS.get(a.workload, 60)
-    vals = []
-    samples = []
-    for i in range(a.warmup + a.steps):
-        s = cpu_sample(a.workload, a.cpu_scale, a.omega)
-        if i >= a.warmup:
-            samples.append(s)
-            vals.append(cpu_extrapolate(s, dofs_full, its_full))
-    v = statistics.median(vals)
-    s = samples[0]
+    threads = cpu_threads(a)
+    smp = cpu_worker({"mode": "iters", "workload": a.workload, "scale": a.cpu_scale, "omega": a.omega,
+                      "n": a.warmup + a.steps}, threads)
+    iter_times = smp["iter_times_s"][a.warmup:]
+    iter_s = statistics.median(iter_times)
+    v = cpu_extrapolate(smp, iter_s, dofs_full, its_full)
+    sample = (f"NumPy oracle ({threads} BLAS/OpenMP threads): {a.steps} timed PCG iterations from x = 0 on the same "
+              f"generator at {smp['shape']} (y, x, z; {smp['voids']} voids, {smp['levels']} levels, {smp['dofs']} DOFs), "
+              f"median {iter_s:.3f} s per iteration; setup {smp['setup_s']:.2f} s of which the coarsest factorisation "
+              f"{smp['coarsest_factor_s']:.2f} s; extrapolated to {dofs_full} DOFs and {its_full} iterations")
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": a.gpus, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": a.workload, "dofs": dofs_full, "levels": L, "omega": a.omega, "tol": 1e-3},
-        "cpu_baseline": {"value": v, "unit": "s", "cores": os.cpu_count(), "kind": "port",
-                         "sample": f"NumPy oracle: setup + {s['its']} CG iterations on the same generator at "
-                                   f"{s['shape']} ({s['dofs']} DOFs, {s['levels']} levels), scaled linearly by DOFs "
-                                   f"to {dofs_full} DOFs and {its_full} iterations"},
+        "extrapolated": True,
+        "measured": {"sample_dofs": smp["dofs"], "sample_shape_y_x_z": smp["shape"], "sample_levels": smp["levels"],
+                     "iteration_s_median": iter_s, "iteration_s": iter_times, "setup_s": smp["setup_s"],
+                     "coarsest_factor_s": smp["coarsest_factor_s"], "threads": threads,
+                     "thread_env": smp["threads"], "blas_threads": smp.get("blas_threads"),
+                     "timed_s": float(sum(iter_times))},
+        "cpu_baseline": {"value": v, "unit": "s", "cores": threads, "kind": "port", "extrapolated": True,
+                         "sample": sample},
         "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -234,6 +296,51 @@ def pinned_like(arr):
     order = "F" if arr.flags.f_contiguous and not arr.flags.c_contiguous else "C"
     out = flat.reshape(arr.shape, order=order)
     out[...] = arr
+    return out
+
+
+def config1_comparison(a, threads: int, stream) -> dict:
+    """The 42 x 37 x 64 workload (20 voids, 4 levels) solved to tolerance by
+    the CPU oracle on the host cores (measured, not extrapolated) and by the
+    GPU in both precisions on the same inputs, with the GPU displacements'
+    error against the oracle's."""
+    import numpy as np
+    import torch
+    from gmgs import Solver, synthetic
+
+    name = "block42_fp64"
+    fd, u_path = tempfile.mkstemp(suffix=".npy")
+    os.close(fd)
+    try:
+        ref = cpu_worker({"mode": "full", "workload": name, "scale": 1.0, "omega": a.omega, "u_path": u_path},
+                         threads)
+        u_ref = np.load(u_path)
+    finally:
+        os.unlink(u_path)
+    vox, fixed, loads, L, _ = synthetic.make(name)
+    out = {"workload": name, "dofs": ref["dofs"], "levels": ref["levels"], "cpu_threads": threads,
+           "cpu_setup_s": ref["setup_s"], "cpu_solve_s": ref["solve_s"], "cpu_total_s": ref["setup_s"] + ref["solve_s"],
+           "cpu_iterations": ref["iterations"], "cpu_relres": ref["relres"], "thread_env": ref["threads"],
+           "blas_threads": ref.get("blas_threads")}
+    for prec in ("fp64", "mixed"):
+        s = Solver(vox, omega=a.omega, num_levels=L, tol=1e-3, precision=prec)
+        s.set_stream(stream.cuda_stream)
+        s.set_bc(fixed, loads)
+        u = s.solve()
+        for _ in range(2):
+            s.solve_dev(None)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(5):
+            s.solve_dev(None)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out[f"gpu_{prec}_solve_s"] = e0.elapsed_time(e1) / 5 / 1e3
+        out[f"gpu_{prec}_iterations"] = s.iterations
+        out[f"gpu_{prec}_displacement_rel_err_vs_cpu"] = float(np.linalg.norm(u - u_ref) / np.linalg.norm(u_ref))
+        s.close()
+    out["speedup_cpu_solve_vs_gpu_mixed"] = out["cpu_solve_s"] / out["gpu_mixed_solve_s"]
     return out
 
 
@@ -389,13 +496,23 @@ def run_gmgs(a):
                "d2h_bytes_per_step": int(u.nbytes), "phases_ms": phases}
 
     cpu = None
+    cpu_config1 = None
     if rank == 0 and not a.no_cpu:
-        smp = cpu_sample(a.workload, a.cpu_scale, a.omega)
-        v = cpu_extrapolate(smp, dofs, its)
-        cpu = {"value": v, "unit": "s", "cores": 1, "kind": "port",
-               "sample": f"NumPy oracle: setup + {smp['its']} CG iterations on the same generator at {smp['shape']} "
-                         f"({smp['dofs']} DOFs, {smp['levels']} levels) = {smp['setup_s']:.1f} s + "
-                         f"{smp['iter_s']:.2f} s/iteration, scaled linearly by DOFs to {dofs} DOFs and {its} iterations"}
+        threads = cpu_threads(a)
+        smp = cpu_worker({"mode": "iters", "workload": a.workload, "scale": a.cpu_scale, "omega": a.omega, "n": 3},
+                         threads)
+        iter_s = statistics.median(smp["iter_times_s"][1:])
+        v = cpu_extrapolate(smp, iter_s, dofs, its)
+        cpu = {"value": v, "unit": "s", "cores": threads, "kind": "port", "extrapolated": True,
+               "sample": f"NumPy oracle ({threads} BLAS/OpenMP threads): setup {smp['setup_s']:.2f} s (coarsest "
+                         f"factorisation {smp['coarsest_factor_s']:.2f} s) + 2 timed PCG iterations "
+                         f"({iter_s:.3f} s each) on the same generator at {smp['shape']} (y, x, z; {smp['levels']} "
+                         f"levels, {smp['dofs']} DOFs), extrapolated to {dofs} DOFs and {its} iterations",
+               "measured": {"sample_dofs": smp["dofs"], "iteration_s": iter_s, "setup_s": smp["setup_s"],
+                            "coarsest_factor_s": smp["coarsest_factor_s"], "thread_env": smp["threads"],
+                            "blas_threads": smp.get("blas_threads")}}
+        if not a.no_cpu_config1:
+            cpu_config1 = config1_comparison(a, threads, stream)
 
     if rank != 0:
         return
@@ -427,6 +544,7 @@ def run_gmgs(a):
         "breakdown": breakdown,
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
+        "cpu_config1": cpu_config1,
         "e2e": e2e,
         "device_bytes": s.device_bytes,
         "generate_s": t_gen,

@@ -7,8 +7,6 @@
 // cudaMalloc / cudaFree.  The block partials and the arrival counter of the
 // deterministic reduction live in a fixed static device array instead of
 // per-handle scratch, so the call allocates nothing.
-#include <mutex>
-
 #include "gmgs_internal.cuh"
 
 namespace gmgs {
@@ -73,34 +71,20 @@ __global__ void __launch_bounds__(kThreads) k_dot_noalloc(const double* __restri
     }
 }
 
-// Device address of the static scratch, looked up once per device with that
-// device current (a host-side reference to the array's name is not a device
-// address).
-std::mutex g_scratch_mutex;
-void* g_scratch_ptr[256] = {};
-
+// Device address of the static scratch for the current device and context.
+// A host-side reference to the array's name is not a device address, so the
+// address is looked up on every call: after the module is loaded on a device
+// (the first call there) the lookup is a cheap table query, and a pointer
+// cached by device ordinal could outlive a cudaDeviceReset or a change of
+// the current context.
 int scratch_for_current_device(double** out) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) {
-        gmgs::set_thread_error(std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+        gmgs::set_thread_error(std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
         return GMGS_ERR_CUDA;
     }
-    if (dev < 0 || dev >= 256) {
-        gmgs::set_thread_error("device ordinal out of range");
-        return GMGS_ERR_CUDA;
-    }
-    std::lock_guard<std::mutex> lock(g_scratch_mutex);
-    if (!g_scratch_ptr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p) {
-            gmgs::set_thread_error(std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-            return GMGS_ERR_CUDA;
-        }
-        g_scratch_ptr[dev] = p;
-    }
-    *out = static_cast<double*>(g_scratch_ptr[dev]);
+    *out = static_cast<double*>(p);
     return GMGS_OK;
 }
 

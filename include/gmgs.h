@@ -159,16 +159,20 @@ int gmgs_dot_dev(gmgs_handle* h, const double* x_dev, const double* y_dev, int64
  * buffers, a framework whose caching allocator must see every allocation) and
  * code paths that cannot afford the implicit device synchronisation of
  * cudaMalloc / cudaFree.  It needs no handle and calls no allocating routine.
- * Computes the deterministic FP64 inner product of two device vectors of n
- * doubles into the device scalar *result_dev, asynchronously on `stream`
- * (a cudaStream_t; NULL = the legacy default stream).
+ * Computes the FP64 inner product of two device vectors of n doubles into
+ * the device scalar *result_dev, asynchronously on `stream` (a cudaStream_t;
+ * NULL = the legacy default stream).  The result is deterministic for a given
+ * n on any GPU (fixed chunks of 8,192 elements, partials summed in chunk
+ * order) but not bit-identical to gmgs_dot_dev, which partitions the vectors
+ * differently; the two agree to rounding.
  * Scratch: a fixed 512 KiB static device array inside libgmgs (65,536 block
  * partials and an arrival counter), held by every GPU that loads the library
  * until the process exits.  n must not exceed GMGS_DOT_NOALLOC_MAX_N
  * (65,536 blocks x 8,192 elements); longer vectors get
- * GMGS_ERR_INVALID_ARGUMENT (use gmgs_dot_dev).  The first call on a device
- * looks up the array's device address (cudaGetSymbolAddress) with that device
- * current, so make that first call before any stream capture.  All calls
+ * GMGS_ERR_INVALID_ARGUMENT (use gmgs_dot_dev).  Every call looks up the
+ * array's device address (cudaGetSymbolAddress) for the current device; the
+ * first call on a device also loads the library's kernels there, so make that
+ * first call before any stream capture.  All calls
  * share the array and each clears the counter it needs before its kernel
  * runs; calls that overlap on the GPU (several streams or host threads at
  * once) race on the array and must be serialised by the caller. */

@@ -2,8 +2,8 @@
 
     python tests/golden/make_voxelize_golden.py [REFERENCE_DIR]
 
-REFERENCE_DIR defaults to $GMGS_REFERENCE_DIR, else /root/reference (the
-read-only GMGS-3D checkout).
+REFERENCE_DIR is a GMGS-3D checkout; without the argument the script reads
+it from $GMGS_REFERENCE_DIR and stops when neither is given.
 For every model and resolution of the reference README's statistics table
 (README.md:29-41) this voxelises data/<model>.ply with the oracle restatement
 (oracle/voxelize.py), discretises it with the oracle (DiscretizeDesignDomain),
@@ -36,13 +36,16 @@ README = {
 
 
 def reference_dir():
-    """The reference checkout: $GMGS_REFERENCE_DIR, else /root/reference."""
+    """The reference checkout named by $GMGS_REFERENCE_DIR, or None."""
     import os
-    return Path(os.environ.get("GMGS_REFERENCE_DIR", "/root/reference"))
+    d = os.environ.get("GMGS_REFERENCE_DIR")
+    return Path(d) if d else None
 
 
 def main():
     ref = Path(sys.argv[1]) if len(sys.argv) > 1 else reference_dir()
+    if ref is None:
+        raise SystemExit("give the GMGS-3D checkout as an argument or in $GMGS_REFERENCE_DIR")
     out = {}
     for model, table in README.items():
         out[model] = {}

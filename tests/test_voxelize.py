@@ -17,7 +17,7 @@ GOLDEN = Path(__file__).resolve().parent / "golden"
 sys.path.insert(0, str(GOLDEN))
 import make_voxelize_golden as MK   # noqa: E402
 
-REFERENCE = MK.reference_dir()      # the reference checkout with its meshes (absent on GPU hosts)
+REFERENCE = MK.reference_dir()      # $GMGS_REFERENCE_DIR: a checkout with the reference's meshes, or None
 
 
 def _golden():
@@ -59,7 +59,8 @@ def test_golden_occupancy_discretizes_to_readme_dofs(name, dofs):
     assert 3 * fine.numNodes == dofs
 
 
-@pytest.mark.skipif(not (REFERENCE / "data" / "kitten.ply").exists(), reason="reference meshes not present")
+@pytest.mark.skipif(REFERENCE is None or not (REFERENCE / "data" / "kitten.ply").exists(),
+                    reason="reference meshes not present (set GMGS_REFERENCE_DIR)")
 @pytest.mark.parametrize("name", ["kitten", "parts"])
 def test_oracle_reproduces_golden_from_the_reference_mesh(name):
     vol, _, grid = V.create_voxelized_model(REFERENCE / "data" / f"{name}.ply", 64)

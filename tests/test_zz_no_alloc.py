@@ -22,6 +22,9 @@ def handle_solver():
     return Solver(np.ones((8, 8, 8), np.int32), num_levels=2)
 
 
+# 3,000,001 is not a multiple of the 8,192-element chunk and spans 367
+# blocks, more than the 256 threads of the last block: its strided walk over
+# the partials runs more than once.
 @pytest.mark.parametrize("n", [1, 8192, 8193, 3_000_001])
 def test_noalloc_dot_matches_handle_dot_twice(handle_solver, n):
     torch = pytest.importorskip("torch")
@@ -61,3 +64,24 @@ def test_noalloc_dot_rejects_oversize_and_bad_arguments():
     assert lib.gmgs_dot_dev_noalloc(p, p, 0, o, None) == 0
     torch.cuda.synchronize()
     assert out.item() == 0.0
+
+
+def test_noalloc_dot_allocates_no_device_memory():
+    """The property the entry point exists for: after a first call on the
+    device, further calls leave the device's free memory unchanged."""
+    torch = pytest.importorskip("torch")
+    from gmgs import _lib
+    lib = _lib.load()
+    n = 1_000_003
+    x = torch.ones(n, dtype=torch.float64, device="cuda")
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    args = (C.c_void_p(x.data_ptr()), C.c_void_p(x.data_ptr()), n, C.c_void_p(out.data_ptr()), None)
+    assert lib.gmgs_dot_dev_noalloc(*args) == 0
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(5):
+        assert lib.gmgs_dot_dev_noalloc(*args) == 0
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    assert out.item() == float(n)

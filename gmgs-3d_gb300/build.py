@@ -20,7 +20,8 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = ROOT / "_build" / "gmgs"
 LIB = PKG / "gmgs" / "libgmgs.so"
-SOURCES = ["api.cu", "setup.cu", "operators.cu", "solver.cu", "post.cu", "fine.cu", "noalloc.cu", "voxelize.cu", "coarse.cu"]
+SOURCES = ["api.cu", "setup.cu", "operators.cu", "solver.cu", "post.cu", "fine.cu", "tc.cu", "noalloc.cu", "voxelize.cu",
+           "coarse.cu"]
 # the voxeliser decides inside/outside by exact FP64 comparisons: no FMA contraction
 FILE_FLAGS = {"voxelize.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

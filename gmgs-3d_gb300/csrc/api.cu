@@ -169,11 +169,11 @@ int64_t model_bytes(const gmgs::Model& M) {
     for (const auto& lv : M.levels)
         for (const gmgs::DevBuf* d : {&lv.emask, &lv.nflag, &lv.etype, &lv.escale64, &lv.escale32, &lv.Ks64, &lv.Ks32,
                                       &lv.kslot, &lv.diag64, &lv.diag32, &lv.wdinv32, &lv.emask8, &lv.perel_nodes, &lv.node_slot, &lv.elem_slot,
-                                      &lv.vr, &lv.vrp, &lv.vdx, &lv.vx, &lv.vy, &lv.tile_occ})
+                                      &lv.vr, &lv.vrp, &lv.vdx, &lv.vx, &lv.vy, &lv.tile_occ, &lv.tc_occ})
             b += (int64_t)d->bytes;
     for (const gmgs::DevBuf* d : {&M.ke0_dev, &M.rho, &M.F, &M.U, &M.free_idx, &M.cb.sinv, &M.cb.g, &M.cb.partial, &M.cb.ticket, &M.cvec_in, &M.cvec_out,
                                   &M.cg_x, &M.cg_r, &M.cg_p, &M.cg_dx, &M.cg_q64, &M.cg_y64, &M.cg_z64, &M.cg_q32,
-                                  &M.cg_y32, &M.cg_z32, &M.cg_r32, &M.cg_r32b, &M.cg_pa, &M.cg_pb, &M.scal, &M.dot_partials, &M.dot_ticket})
+                                  &M.cg_y32, &M.cg_z32, &M.cg_r32, &M.cg_r32b, &M.cg_pa, &M.cg_pb, &M.scal, &M.dot_partials, &M.dot_ticket, &M.tc_err})
         b += (int64_t)d->bytes;
     return b;
 }

@@ -223,6 +223,20 @@ __device__ __forceinline__ void boundary_s(const FineLevel& L, const Coef32& cf,
 
 constexpr uint8_t NF_PEREL = 32;     // node touches an element with its own stored matrix
 
+// B operand of the tensor-core element kernels (tc.cu): Ke (row = output DOF)
+// as TF32 in the tensor cores' K-major no-swizzle shared-memory layout, N
+// padded to 32 rows.
+struct TcCoef {
+    float B[32 * 24];
+};
+void make_tc_coef(const double* ke_rows, TcCoef& c);
+// V-cycle down-sweep out = r - A (w r) on the tensor cores, element form
+// (err: device flag set when a tensor-core wait runs out)
+void launch_tc_vdown(Ctx& c, const FineLevel& L, const TcCoef& cf, const float* r32, const float* wdinv, float* out,
+                     int* err);
+size_t tc_tile_occ_bytes(const Grid& g);
+void launch_tc_tile_occ(Ctx& c, const Grid& g, const uint8_t* nflag, uint8_t* occ);
+
 void make_stencil(const double* ke_rows, Coef32& cf);
 int fine_grid_blocks(const Grid& g);
 int up32_grid_blocks(const Grid& gf);

@@ -168,6 +168,7 @@ struct Level {
     DevBuf wdinv32;           // mixed path: omega / diag in FP32
     DevBuf emask8;            // mixed path: per-node mask of the 8 surrounding solid elements
     DevBuf perel_nodes;       // slots of nodes touching an element with its own stored matrix
+    DevBuf tc_occ;            // mixed path: per 31x7 node tile (tensor-core kernels) and z plane, 1 if solid
     int64_t n_perel = 0;
 };
 

@@ -837,6 +837,7 @@ void build_operators(Model& M) {
     std::copy(KeT, KeT + KE, M.ke0_rows);
     make_mat_coef(KeT, M.mc64, M.mc32);
     make_stencil(KeT, M.coef);
+    make_tc_coef(KeT, M.tcoef);
     for (int l = 0; l < L; ++l) {
         Level& lv = M.levels[l];
         const bool uniform_ok = !(l == 0 && lv.escale64.p);

@@ -37,6 +37,9 @@ struct Model {
     DevBuf cg_q32, cg_y32, cg_z32, cg_r32;                     // mixed path
     DevBuf cg_r32b, cg_pa, cg_pb;                              // mixed path double buffers
     Coef32 coef{};                                             // FP32 stencil + element matrix
+    TcCoef tcoef{};                                            // Ke as the tensor cores' B operand
+    DevBuf tc_err;         // int: set when a tensor-core wait ran out
+    bool use_tc = false;   // V-cycle down-sweeps on the tensor cores (environment GMGS_TC)
     DevBuf scal;           // device scalars (see solver.cu)
     DevBuf dot_partials, dot_ticket;
     // CUDA graphs of the mixed PCG iteration body (one per parity), valid for

@@ -55,6 +55,8 @@ void alloc_work(Model& M) {
                 launch_emask8(c, lv.g, lv.emask.as<uint8_t>(), lv.emask8.as<uint8_t>());
                 if (lv.tile_occ.bytes < tile_occ_bytes(lv.g)) lv.tile_occ = dalloc(tile_occ_bytes(lv.g));
                 launch_tile_occ(c, lv.g, lv.nflag.as<uint8_t>(), lv.tile_occ.as<uint8_t>());
+                if (lv.tc_occ.bytes < tc_tile_occ_bytes(lv.g)) lv.tc_occ = dalloc(tc_tile_occ_bytes(lv.g));
+                launch_tc_tile_occ(c, lv.g, lv.nflag.as<uint8_t>(), lv.tc_occ.as<uint8_t>());
             }
         }
     }
@@ -76,6 +78,7 @@ void alloc_work(Model& M) {
         zalloc(c, M.cg_z64, n3 * 8);
     }
     zalloc(c, M.scal, SC_N * sizeof(double));
+    if (mixed) zalloc(c, M.tc_err, sizeof(int));
     M.dot_blocks = M.ctx.num_sms * 4;
     const int maxb = std::max({M.dot_blocks, fine_grid_blocks(M.levels[0].g), up32_grid_blocks(M.levels[0].g)});
     zalloc(c, M.dot_partials, (size_t)maxb * sizeof(double));
@@ -86,6 +89,25 @@ void alloc_work(Model& M) {
 
 static DotScratch dots(Model& M) {
     return DotScratch{M.dot_partials.as<double>(), M.dot_ticket.as<unsigned int>(), M.dot_blocks};
+}
+
+// V-cycle down-sweeps on the tensor cores when the environment sets GMGS_TC=1
+static bool tc_enabled() {
+    const char* e = std::getenv("GMGS_TC");
+    return e && e[0] == '1';
+}
+
+// A tensor-core kernel whose wait on its MMA ran out sets the device flag;
+// the solve reports it instead of returning a result computed without it.
+static void check_tc(Model& M) {
+    if (!M.use_tc || !M.tc_err.p) return;
+    int flag = 0;
+    GMGS_CUDA(cudaMemcpyAsync(&flag, M.tc_err.p, sizeof(int), cudaMemcpyDeviceToHost, M.ctx.stream));
+    GMGS_CUDA(cudaStreamSynchronize(M.ctx.stream));
+    if (flag) {
+        GMGS_CUDA(cudaMemsetAsync(M.tc_err.p, 0, sizeof(int), M.ctx.stream));
+        throw Error(GMGS_ERR_CUDA, "a tensor-core kernel's wait for its MMA timed out");
+    }
 }
 
 // One V(1,1) cycle, Vcycle.m:1-36: down-sweep Jacobi with residual update and
@@ -128,9 +150,11 @@ static void vcycle32(Model& M, const float* r32, float* z, bool with_dot, int do
 void vcycle_apply(Model& M, const double* r, double* z) {
     const int64_t n3 = 3 * M.levels[0].g.slots;
     if (M.prm.precision == GMGS_MIXED) {
+        M.use_tc = tc_enabled();
         launch_copy<float, double>(M.ctx, n3, M.cg_r32.as<float>(), r);
         vcycle32(M, M.cg_r32.as<float>(), M.cg_z32.as<float>(), false, 0);
         launch_copy<double, float>(M.ctx, n3, z, M.cg_z32.as<float>());
+        check_tc(M);
     } else {
         vcycle<double>(M, r, z);
     }
@@ -193,8 +217,15 @@ static void vcycle32(Model& M, const float* r32, float* z, bool with_dot, int do
         }
         if (l == 1) c.mark(PK_COARSE, false);
         const FineLevel fl = fine_level(lv);
-        if (l == 0) launch_l0<FM_VCYCLE_DOWN>(M, fl, a);
-        else if (lv.n_perel < lv.n_node) launch_fine<FM_VCYCLE_DOWN>(c, fl, M.coef, a);
+        if (M.use_tc && lv.n_perel < lv.n_node) {
+            FineLevel ft = fl;
+            ft.tile_occ = lv.tc_occ.as<uint8_t>();
+            launch_tc_vdown(c, ft, M.tcoef, a.r32, a.wdinv, a.out32, M.tc_err.as<int>());
+        } else if (l == 0) {
+            launch_l0<FM_VCYCLE_DOWN>(M, fl, a);
+        } else if (lv.n_perel < lv.n_node) {
+            launch_fine<FM_VCYCLE_DOWN>(c, fl, M.coef, a);
+        }
         if (lv.n_perel > 0)
             launch_perel_vdown(c, fl, M.coef, lv.perel_nodes.as<int32_t>(), (int)lv.n_perel, a.r32, a.wdinv,
                                a.out32);
@@ -279,6 +310,7 @@ static bool capture_iteration_graphs(Model& M, Body& body) {
 
 static int pcg_mixed(Model& M, const double* b, double* x, int32_t* iters_out, double* relres_out, double* hist) {
     Ctx& c = M.ctx;
+    M.use_tc = tc_enabled();
     Level& l0 = M.levels[0];
     const int64_t n3 = 3 * l0.g.slots;
     double* scal = M.scal.as<double>();
@@ -423,6 +455,7 @@ static int pcg_mixed(Model& M, const double* b, double* x, int32_t* iters_out, d
     // that does not run; its inputs (r32 it read, q, alpha) are still in place
     launch_drop_last_dx(c, n3, x, r32b, q, l0.wdinv32.as<float>(), scal, its & 1, 0);
     GMGS_CUDA(cudaStreamSynchronize(c.stream));
+    check_tc(M);
     if (status == GMGS_ERR_MAX_ITERATIONS && M.prm.verbose) std::printf("Exceed the maximum iterate numbers\n");
     if (iters_out) *iters_out = its;
     if (relres_out) *relres_out = resnorm;

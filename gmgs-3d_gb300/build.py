@@ -3,7 +3,11 @@
     python gmgs-3d_gb300/build.py [--debug] [--jobs N]
 
 Each .cu translation unit compiles in parallel into _build/, then one shared
-library is linked into gmgs-3d_gb300/gmgs/libgmgs.so.
+library is linked into gmgs-3d_gb300/gmgs/libgmgs.so.  --debug builds the
+checked library gmgs-3d_gb300/gmgs/libgmgs_checked.so instead (GMGS_CHECKED:
+every instrumented gather, scatter and shared-memory access tests its index
+and the C ABI reports an out-of-range one; host code at -O0 -g); load it by
+setting GMGS_LIB to its path.
 """
 from __future__ import annotations
 
@@ -20,6 +24,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = ROOT / "_build" / "gmgs"
 LIB = PKG / "gmgs" / "libgmgs.so"
+LIB_CHECKED = PKG / "gmgs" / "libgmgs_checked.so"
 SOURCES = ["api.cu", "setup.cu", "operators.cu", "solver.cu", "post.cu", "fine.cu", "tc.cu", "noalloc.cu", "voxelize.cu",
            "coarse.cu"]
 # the voxeliser decides inside/outside by exact FP64 comparisons: no FMA contraction
@@ -51,7 +56,7 @@ def compile_one(src: str, debug: bool) -> Path:
     out = obj_dir(debug) / (Path(src).stem + ".o")
     srcp = CSRC / src
     deps = [srcp] + list(CSRC.glob("*.cuh")) + [ROOT / "include" / "gmgs.h"]
-    if out.exists() and all(out.stat().st_mtime >= d.stat().st_mtime for d in deps) and not debug:
+    if out.exists() and all(out.stat().st_mtime >= d.stat().st_mtime for d in deps):
         return out
     cmd = [nvcc(), *flags(debug), *FILE_FLAGS.get(src, []), "-c", str(srcp), "-o", str(out)]
     res = subprocess.run(cmd, capture_output=True, text=True)
@@ -68,17 +73,14 @@ def build(debug: bool = False, jobs: int | None = None) -> Path:
     with cf.ThreadPoolExecutor(max_workers=jobs or min(8, len(srcs))) as ex:
         objs = list(ex.map(lambda s: compile_one(s, debug), srcs))
     newest = max(o.stat().st_mtime for o in objs)
-    mode = "debug" if debug else "release"
-    stamp = BUILD / "libgmgs.mode"      # the mode the in-tree library was last linked in
-    if (LIB.exists() and LIB.stat().st_mtime >= newest and not debug and stamp.exists()
-            and stamp.read_text() == mode):
-        return LIB
-    cmd = [nvcc(), *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcudart"]
+    lib = LIB_CHECKED if debug else LIB
+    if lib.exists() and lib.stat().st_mtime >= newest:
+        return lib
+    cmd = [nvcc(), *ARCH, "-shared", "-o", str(lib), *map(str, objs), "-lcudart"]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
-    stamp.write_text(mode)
-    return LIB
+    return lib
 
 
 if __name__ == "__main__":

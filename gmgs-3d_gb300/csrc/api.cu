@@ -33,7 +33,16 @@ double ms_since(Clock::time_point t0) {
 template <class F>
 int guarded(gmgs_handle* h, F&& f) {
     try {
-        return f();
+        const int st = f();
+#ifdef GMGS_CHECKED
+        std::string m;
+        if (gmgs::chk::report(m)) {
+            g_last_error = m;
+            if (h) h->M.err = m;
+            return GMGS_ERR_CUDA;
+        }
+#endif
+        return st;
     } catch (const gmgs::Error& e) {
         g_last_error = e.what();
         if (h) h->M.err = e.what();
@@ -218,6 +227,40 @@ int solve_impl(gmgs_handle* h, double* U_host, double* U_dev, int32_t* iters, do
 namespace gmgs {
 // error message for entry points that run without a handle
 void set_thread_error(const std::string& msg) { g_last_error = msg; }
+
+namespace chk {
+const char* site_name(int site) {
+    static const char* const names[SITE_COUNT] = {
+        "none", "k_fine field staging", "k_fine node operands", "k_fine node flags", "k_fine element data",
+        "k_fine element matrices", "k_fine shared ring", "k_fine outputs", "k_up32 fine operands",
+        "k_up32 coarse values", "k_up32 output", "k_perel_vdown node list", "k_perel_vdown element data",
+        "k_perel_vdown vectors", "k_perel_vdown element matrices", "k_perel_vdown output", "k_tc_vdown field staging",
+        "k_tc_vdown element data", "k_tc_vdown node operands", "k_tc_vdown shared ring",
+        "k_tc_vdown element-output buffer", "k_tc_vdown output", "k_matvec input gather", "k_matvec element data",
+        "k_matvec output", "k_restrict", "k_prolong_post", "stress displacement gather", "stress outputs",
+        "k_grad"};
+    return site > 0 && site < SITE_COUNT ? names[site] : "unknown site";
+}
+#ifdef GMGS_CHECKED
+static std::vector<Reader>& readers() {
+    static std::vector<Reader> v;
+    return v;
+}
+void add_reader(Reader r) { readers().push_back(r); }
+bool report(std::string& msg) {
+    cudaDeviceSynchronize();
+    bool any = false;
+    for (Reader r : readers()) {
+        std::string m;
+        if (r(m) && !any) {
+            msg = m;
+            any = true;
+        }
+    }
+    return any;
+}
+#endif
+}  // namespace chk
 }  // namespace gmgs
 
 extern "C" {

@@ -68,18 +68,22 @@ void make_stencil(const double* ke_rows, Coef32& cf) {
 // input field at one point (3 components) from the kernel's inputs
 template <int MODE>
 __device__ __forceinline__ void field_at(const FineArgs& a, int S, int s, float beta, float alpha, float v[3]) {
+    const long long n3 = 3ll * S;
+    constexpr int F = chk::FINE_FIELD;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         const int i = s + c * S;
         if (MODE == FM_PLAIN) {
-            v[c] = a.v[i];
+            v[c] = chk::ld(a.v, i, n3, F);
         } else if (MODE == FM_VCYCLE_DOWN) {
-            v[c] = a.r32[i] * a.wdinv[i];
+            v[c] = chk::ld(a.r32, i, n3, F) * chk::ld(a.wdinv, i, n3, F);
         } else if (MODE == FM_CG_UPDATE_JACOBI) {
-            const float rm = a.first ? a.r32[i] : fmaf(-alpha, a.q32[i], a.r32[i]);
-            v[c] = rm * a.wdinv[i];
+            const float r = chk::ld(a.r32, i, n3, F);
+            const float rm = a.first ? r : fmaf(-alpha, chk::ld(a.q32, i, n3, F), r);
+            v[c] = rm * chk::ld(a.wdinv, i, n3, F);
         } else {   // FM_CG_DIRECTION
-            v[c] = a.first ? a.z32[i] : fmaf(beta, a.pold[i], a.z32[i]);
+            const float z = chk::ld(a.z32, i, n3, F);
+            v[c] = a.first ? z : fmaf(beta, chk::ld(a.pold, i, n3, F), z);
         }
     }
 }
@@ -95,17 +99,19 @@ struct EpiData {
 
 template <int MODE>
 __device__ __forceinline__ void epi_fetch(const FineArgs& a, int S, int n, EpiData& d) {
+    const long long n3 = 3ll * S;
+    constexpr int E = chk::FINE_EPI;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         const int i = n + c * S;
-        if (MODE == FM_VCYCLE_DOWN) d.r[c] = a.r32[i];
+        if (MODE == FM_VCYCLE_DOWN) d.r[c] = chk::ld(a.r32, i, n3, E);
         if (MODE == FM_CG_UPDATE_JACOBI) {
-            d.r[c] = a.r32[i];
-            d.r64[c] = a.r64[i];
-            d.x64[c] = a.x64[i];
+            d.r[c] = chk::ld(a.r32, i, n3, E);
+            d.r64[c] = chk::ld((const double*)a.r64, i, n3, E);
+            d.x64[c] = chk::ld((const double*)a.x64, i, n3, E);
             if (!a.first) {
-                d.q[c] = a.q32[i];
-                d.pp[c] = a.pold[i];
+                d.q[c] = chk::ld(a.q32, i, n3, E);
+                d.pp[c] = chk::ld(a.pold, i, n3, E);
             }
         }
     }
@@ -168,8 +174,13 @@ __global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? 3 : 5)
         if (zok && hcol) field_at<MODE>(a, S, hbase + iz * sz, beta, alpha, vh);
     };
     auto store = [&](float* r, const float vc[3], const float vh[3]) {
-        r[pc] = vc[0]; r[pc + PLANE] = vc[1]; r[pc + 2 * PLANE] = vc[2];
-        if (tid < NHALO) { r[ph] = vh[0]; r[ph + PLANE] = vh[1]; r[ph + 2 * PLANE] = vh[2]; }
+        constexpr long long R = 3 * PLANE;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) chk::st(r, pc + c * PLANE, R, chk::FINE_RING, vc[c]);
+        if (tid < NHALO) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) chk::st(r, ph + c * PLANE, R, chk::FINE_RING, vh[c]);
+        }
     };
 
     float vc[3], vh[3];
@@ -182,8 +193,8 @@ __global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? 3 : 5)
     const bool own = cy <= g.ny && cx <= g.nx;
     uint32_t f_next = 0, e8_next = 0;
     if (own) {
-        f_next = L.nflag[cbase + zb * sz];
-        e8_next = L.emask8[cbase + zb * sz];
+        f_next = chk::ld(L.nflag, cbase + zb * sz, g.slots, chk::FINE_FLAGS);
+        e8_next = chk::ld(L.emask8, cbase + zb * sz, g.slots, chk::FINE_FLAGS);
     }
     Kahan dot;
 #pragma unroll 1
@@ -193,8 +204,8 @@ __global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? 3 : 5)
         if (iz + 2 <= g.nz + 1) fetch(iz + 2, vc, vh);
         const uint32_t f = f_next, e8 = e8_next;
         if (own && iz + 1 < ze) {
-            f_next = L.nflag[cbase + (iz + 1) * sz];
-            e8_next = L.emask8[cbase + (iz + 1) * sz];
+            f_next = chk::ld(L.nflag, cbase + (iz + 1) * sz, g.slots, chk::FINE_FLAGS);
+            e8_next = chk::ld(L.emask8, cbase + (iz + 1) * sz, g.slots, chk::FINE_FLAGS);
         }
         const float* P0 = ring[(iz - 1 + RING) % RING];
         const float* P1 = ring[iz % RING];
@@ -213,14 +224,16 @@ __global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? 3 : 5)
             if (f & NF_FIX_X) y[0] = 0.f;
             if (f & NF_FIX_Y) y[1] = 0.f;
             if (f & NF_FIX_Z) y[2] = 0.f;
+            const long long n3 = 3ll * S;
+            constexpr int O = chk::FINE_OUT;
 #pragma unroll
             for (int b = 0; b < 3; ++b) {
                 const int i = n + b * S;
-                const float v = P1[pc + b * PLANE];
+                const float v = chk::ld(P1, pc + b * PLANE, 3 * PLANE, chk::FINE_RING);
                 if (MODE == FM_PLAIN) {
-                    a.out32[i] = y[b];
+                    chk::st(a.out32, i, n3, O, y[b]);
                 } else if (MODE == FM_VCYCLE_DOWN) {
-                    a.out32[i] = ed.r[b] - y[b];                         // r' = r - A (omega D^-1 r)
+                    chk::st(a.out32, i, n3, O, ed.r[b] - y[b]);         // r' = r - A (omega D^-1 r)
                 } else if (MODE == FM_CG_UPDATE_JACOBI) {
                     // previous iteration's update x += alpha p, r -= alpha q (CG_solver.m:32-33),
                     // then this iteration's Jacobi step x += dx, r -= A dx (CG_solver.m:18-19);
@@ -233,14 +246,14 @@ __global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? 3 : 5)
                         rinc = fmaf(alpha, ed.q[b], rinc);
                         rm32 = fmaf(-alpha, ed.q[b], rm32);
                     }
-                    a.x64[i] = ed.x64[b] + (double)xinc;
+                    chk::st(a.x64, i, n3, O, ed.x64[b] + (double)xinc);
                     const double rn = ed.r64[b] - (double)rinc;
-                    a.r64[i] = rn;
-                    a.r32out[i] = (float)rn;
+                    chk::st(a.r64, i, n3, O, rn);
+                    chk::st(a.r32out, i, n3, O, (float)rn);
                     dot.add(rm32 * rm32);
                 } else {
-                    a.pout[i] = v;
-                    a.out32[i] = y[b];                                   // q = A p
+                    chk::st(a.pout, i, n3, O, v);
+                    chk::st(a.out32, i, n3, O, y[b]);                   // q = A p
                     dot.add(v * y[b]);
                 }
             }
@@ -316,22 +329,29 @@ __global__ void __launch_bounds__(256, 4) k_up32(Grid gf, Grid gc, const uint8_t
             for (int k = 0; k < 4; ++k) qa[c][k] = qb[c][k] = 0.f;
         int qa_z = -1;
         auto load_q = [&](int Z, float (&q)[3][4]) {
+            const long long n3c = 3ll * Sc;
+            constexpr int U = chk::UP_COARSE;
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                const float* x = xc + c * Sc + ccol + Z * csz;
-                q[c][0] = x[0]; q[c][1] = x[1]; q[c][2] = x[csx]; q[c][3] = x[csx + 1];
+                const int x = c * Sc + ccol + Z * csz;
+                q[c][0] = chk::ld(xc, x, n3c, U);
+                q[c][1] = chk::ld(xc, x + 1, n3c, U);
+                q[c][2] = chk::ld(xc, x + csx, n3c, U);
+                q[c][3] = chk::ld(xc, x + csx + 1, n3c, U);
             }
         };
         uint8_t flc = 0, fln = 0;
         float wdc[3] = {}, rc[3] = {}, rpc[3] = {}, wdn[3] = {}, rn[3] = {}, rpn[3] = {};
         auto fetch = [&](int z, uint8_t& fl, float (&wd)[3], float (&rr)[3], float (&rq)[3]) {
             const int fs = fcol + z * fsz;
-            fl = nflag[fs];
+            const long long n3f = 3ll * Sf;
+            constexpr int U = chk::UP_FINE;
+            fl = chk::ld(nflag, fs, Sf, U);
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                wd[c] = wdinv[fs + c * Sf];
-                rr[c] = r[fs + c * Sf];
-                rq[c] = rp[fs + c * Sf];
+                wd[c] = chk::ld(wdinv, fs + c * Sf, n3f, U);
+                rr[c] = chk::ld(r, fs + c * Sf, n3f, U);
+                rq[c] = chk::ld(rp, fs + c * Sf, n3f, U);
             }
         };
         bool okc = zb < ze && occ(zb);
@@ -359,7 +379,7 @@ __global__ void __launch_bounds__(256, 4) k_up32(Grid gf, Grid gc, const uint8_t
                         t += (oz & ox & oy) ? qb[c][3] : 0.f;
                         float out = (wdc[c] * rc[c] + w * t) + wdc[c] * rpc[c];
                         if (zero_fixed && (flc & (NF_FIX_X << c))) out = 0.f;
-                        xf[fs + c * Sf] = out;
+                        chk::st(xf, fs + c * Sf, 3ll * Sf, chk::UP_OUT, out);
                         if (DOT) dot.add(rc[c] * out);
                     }
                 }
@@ -444,18 +464,23 @@ __global__ void __launch_bounds__(256) k_perel_vdown(FineLevel L, const __grid_c
     const bool active = node < count;          // whole 8-lane groups; idle groups still shuffle
     const Grid& g = L.g;
     const int S = (int)g.slots, sx = g.py, sz = g.py * g.px;
-    const int n = active ? nodes[node] : 0;
+    const int n = active ? chk::ld(nodes, node, count, chk::PEREL_NODE) : 0;
+    const long long n3 = 3ll * S;
     float acc[3] = {0.f, 0.f, 0.f};
     if (active) {
 #pragma unroll
         for (int e = 0; e < 8; ++e) {
             const int A = e & 1, B = (e >> 1) & 1, C = e >> 2;
             const int es = n - A - B * sx - C * sz;
-            if (!L.emask[es]) continue;         // uniform across the node's lanes
+            if (!chk::ld(L.emask, es, S, chk::PEREL_ELEM)) continue;   // uniform across the node's lanes
             const int ci = corner_of(A, B, C);
-            const int t = L.etype ? L.etype[es] : 0;
+            const int t = L.etype ? chk::ld(L.etype, es, S, chk::PEREL_ELEM) : 0;
             const int nj = es + corner_y(j) + corner_x(j) * sx + corner_z(j) * sz;
-            const float d0 = r[nj] * w[nj], d1 = r[nj + S] * w[nj + S], d2 = r[nj + 2 * S] * w[nj + 2 * S];
+            constexpr int V = chk::PEREL_VEC;
+            const float d0 = chk::ld(r, nj, n3, V) * chk::ld(w, nj, n3, V);
+            const float d1 = chk::ld(r, nj + S, n3, V) * chk::ld(w, nj + S, n3, V);
+            const float d2 = chk::ld(r, nj + 2 * S, n3, V) * chk::ld(w, nj + 2 * S, n3, V);
+            if (t > 0 && !chk::ok(t - 1, L.nK, chk::PEREL_KS)) continue;
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
                 const int off = (3 * ci + a) * 24 + 3 * j;
@@ -476,10 +501,10 @@ __global__ void __launch_bounds__(256) k_perel_vdown(FineLevel L, const __grid_c
         acc[a] += __shfl_xor_sync(0xffffffffu, acc[a], 4);
     }
     if (active && j < 3) {
-        const uint32_t f = L.nflag[n];
+        const uint32_t f = chk::ld(L.nflag, n, S, chk::PEREL_ELEM);
         const float y = j == 0 ? acc[0] : (j == 1 ? acc[1] : acc[2]);
         const int i = n + j * S;
-        out[i] = r[i] - ((f & (NF_FIX_X << j)) ? 0.f : y);
+        chk::st(out, i, n3, chk::PEREL_OUT, chk::ld(r, i, n3, chk::PEREL_VEC) - ((f & (NF_FIX_X << j)) ? 0.f : y));
     }
 }
 

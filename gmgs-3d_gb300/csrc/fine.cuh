@@ -20,6 +20,7 @@ struct FineLevel {
     const uint8_t* emask8;   // per node: bit A + 2B + 4C set when the element at node - (A, B, C) is solid
     const int32_t* etype;    // null: every solid element uses kscale * Ke0
     const float* Ks;         // per-element matrices (FP32), row = output DOF
+    int64_t nK = 0;          // matrices held in Ks (the extent checked builds test element types against)
     const float* escale;     // finest-level element scale or null
     float kscale;
     const uint8_t* tile_occ; // per (z plane, x tile, y tile) of the streaming kernel: any solid node; null = all
@@ -132,7 +133,9 @@ __device__ inline void grid_dot_finish(double v, const DotOut& d, double* sh) {
 template <int RP, int PLANE>
 __device__ __forceinline__ void interior_s(const Coef32& cf, const float* __restrict__ P0, const float* __restrict__ P1,
                                            const float* __restrict__ P2, int p, float& y0, float& y1, float& y2) {
-    const float c0 = P1[p], c1 = P1[p + PLANE], c2 = P1[p + 2 * PLANE];
+    constexpr long long R = 3 * PLANE;   // one ring slot
+    const float c0 = chk::ld(P1, p, R, chk::FINE_RING), c1 = chk::ld(P1, p + PLANE, R, chk::FINE_RING),
+                c2 = chk::ld(P1, p + 2 * PLANE, R, chk::FINE_RING);
     float acc[3] = {0.f, 0.f, 0.f};
 #pragma unroll
     for (int k = 14; k < 27; ++k) {
@@ -140,9 +143,12 @@ __device__ __forceinline__ void interior_s(const Coef32& cf, const float* __rest
         const float* up = off_z(k) > 0 ? P2 : (off_z(k) < 0 ? P0 : P1);
         const float* dn = off_z(k) > 0 ? P0 : (off_z(k) < 0 ? P2 : P1);
         float d[3];
-        d[0] = (up[p + o] - c0) + (dn[p - o] - c0);
-        d[1] = (up[p + o + PLANE] - c1) + (dn[p - o + PLANE] - c1);
-        d[2] = (up[p + o + 2 * PLANE] - c2) + (dn[p - o + 2 * PLANE] - c2);
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            const float cb = b == 0 ? c0 : (b == 1 ? c1 : c2);
+            d[b] = (chk::ld(up, p + o + b * PLANE, R, chk::FINE_RING) - cb) +
+                   (chk::ld(dn, p - o + b * PLANE, R, chk::FINE_RING) - cb);
+        }
 #pragma unroll
         for (int a = 0; a < 3; ++a)
 #pragma unroll
@@ -166,7 +172,9 @@ __device__ __forceinline__ void elem_rows(const Coef32& cf, const float* __restr
         const int dy = corner_y(j) - A, dx = corner_x(j) - B, dz = corner_z(j) - C;
         const float* pl = dz > 0 ? P2 : (dz < 0 ? P0 : P1);
         const int q = p + dy + dx * RP;
-        const float d0 = pl[q] - c0, d1 = pl[q + PLANE] - c1, d2 = pl[q + 2 * PLANE] - c2;
+        constexpr long long R = 3 * PLANE;
+        const float d0 = chk::ld(pl, q, R, chk::FINE_RING) - c0, d1 = chk::ld(pl, q + PLANE, R, chk::FINE_RING) - c1,
+                    d2 = chk::ld(pl, q + 2 * PLANE, R, chk::FINE_RING) - c2;
         float t[3];
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
@@ -193,14 +201,15 @@ __device__ __forceinline__ void boundary_elem(const FineLevel& L, const Coef32& 
     const int es = n - A - B * L.g.py - C * L.g.py * L.g.px;
     float s = L.kscale;
     if (L.etype) {
-        const int t = L.etype[es];
+        const int t = chk::ld(L.etype, es, L.g.slots, chk::FINE_ELEM);
         if (t > 0) {
-            elem_rows<RP, PLANE, A, B, C, false>(cf, L.Ks + (int64_t)(t - 1) * KE, 1.f, P0, P1, P2, p, c0, c1, c2, y0,
-                                                 y1, y2);
+            if (chk::ok(t - 1, L.nK, chk::FINE_KS))
+                elem_rows<RP, PLANE, A, B, C, false>(cf, L.Ks + (int64_t)(t - 1) * KE, 1.f, P0, P1, P2, p, c0, c1, c2,
+                                                     y0, y1, y2);
             return;
         }
     }
-    if (L.escale) s *= L.escale[es];
+    if (L.escale) s *= chk::ld(L.escale, es, L.g.slots, chk::FINE_ELEM);
     elem_rows<RP, PLANE, A, B, C, true>(cf, nullptr, s, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);
 }
 
@@ -208,7 +217,9 @@ template <int RP, int PLANE>
 __device__ __forceinline__ void boundary_s(const FineLevel& L, const Coef32& cf, uint32_t e8, int n,
                                            const float* __restrict__ P0, const float* __restrict__ P1,
                                            const float* __restrict__ P2, int p, float& y0, float& y1, float& y2) {
-    const float c0 = P1[p], c1 = P1[p + PLANE], c2 = P1[p + 2 * PLANE];
+    constexpr long long R = 3 * PLANE;
+    const float c0 = chk::ld(P1, p, R, chk::FINE_RING), c1 = chk::ld(P1, p + PLANE, R, chk::FINE_RING),
+                c2 = chk::ld(P1, p + 2 * PLANE, R, chk::FINE_RING);
     y0 = y1 = y2 = 0.f;
     boundary_elem<RP, PLANE, 0>(L, cf, e8, n, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);
     boundary_elem<RP, PLANE, 1>(L, cf, e8, n, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);

@@ -57,6 +57,76 @@ struct Error : std::runtime_error {
     } while (0)
 
 // ---------------------------------------------------------------------------
+// checked accesses (build.py --debug compiles with GMGS_CHECKED)
+// ---------------------------------------------------------------------------
+// chk::ld / chk::st wrap the gathers, scatters and shared-memory staging of
+// the solver kernels.  In a checked build each one tests its index against the
+// extent of the buffer it touches; an index outside is not accessed (a load
+// gives 0) and is recorded: the number of such accesses and the first one's
+// site and index, in device words of the translation unit.  Every C-ABI call
+// of a checked build then reads those words and fails with GMGS_ERR_CUDA
+// naming the site.  Release builds compile the plain access.
+namespace chk {
+enum Site : int {
+    FINE_FIELD = 1, FINE_EPI, FINE_FLAGS, FINE_ELEM, FINE_KS, FINE_RING, FINE_OUT,
+    UP_FINE, UP_COARSE, UP_OUT, PEREL_NODE, PEREL_ELEM, PEREL_VEC, PEREL_KS, PEREL_OUT,
+    TC_FIELD, TC_ELEM, TC_NODE, TC_RING, TC_EOUT, TC_OUT,
+    MV_X, MV_ELEM, MV_Y, RESTRICT, PROLONG, STRESS_U, STRESS_OUT, GRAD,
+    SITE_COUNT
+};
+const char* site_name(int site);
+#ifdef GMGS_CHECKED
+static __device__ unsigned long long g_first = 0;   // (site << 48) | (index & 2^48-1) of the first violation
+static __device__ unsigned int g_count = 0;
+__device__ __forceinline__ bool ok(long long i, long long n, int site) {
+    if (i >= 0 && i < n) return true;
+    atomicAdd(&g_count, 1u);
+    atomicCAS(&g_first, 0ull, ((unsigned long long)site << 48) | ((unsigned long long)i & 0xFFFFFFFFFFFFull));
+    return false;
+}
+template <typename T>
+__device__ __forceinline__ T ld(const T* p, long long i, long long n, int site) {
+    return ok(i, n, site) ? p[i] : T(0);
+}
+template <typename T, typename V>
+__device__ __forceinline__ void st(T* p, long long i, long long n, int site, V v) {
+    if (ok(i, n, site)) p[i] = (T)v;
+}
+// host: each translation unit registers a reader of its own device words
+using Reader = bool (*)(std::string& msg);
+void add_reader(Reader r);
+bool report(std::string& msg);   // true (and msg) when any kernel recorded a violation
+static bool read_this_unit(std::string& msg) {
+    unsigned long long first = 0;
+    unsigned int count = 0;
+    if (cudaMemcpyFromSymbol(&first, g_first, sizeof(first)) != cudaSuccess ||
+        cudaMemcpyFromSymbol(&count, g_count, sizeof(count)) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    if (!count) return false;
+    const unsigned long long zero = 0;
+    const unsigned int zc = 0;
+    cudaMemcpyToSymbol(g_first, &zero, sizeof(zero));
+    cudaMemcpyToSymbol(g_count, &zc, sizeof(zc));
+    const int site = (int)(first >> 48);
+    long long idx = (long long)(first & 0xFFFFFFFFFFFFull);
+    if (idx & 0x800000000000ll) idx -= 0x1000000000000ll;   // negative indices
+    msg = "checked build: " + std::to_string(count) + " out-of-range access(es), first at " + site_name(site) +
+          " index " + std::to_string(idx);
+    return true;
+}
+static const bool g_reader_added = (add_reader(&read_this_unit), true);
+#else
+__device__ __forceinline__ bool ok(long long, long long, int) { return true; }
+template <typename T>
+__device__ __forceinline__ T ld(const T* p, long long i, long long, int) { return p[i]; }
+template <typename T, typename V>
+__device__ __forceinline__ void st(T* p, long long i, long long, int, V v) { p[i] = (T)v; }
+#endif
+}  // namespace chk
+
+// ---------------------------------------------------------------------------
 // grid geometry
 // ---------------------------------------------------------------------------
 struct Grid {
@@ -113,6 +183,7 @@ struct LevelView {
     const uint8_t* nflag;    // node flags
     const int32_t* etype;    // -1 void, 0 universal (Kc), k>0 -> Ks[k-1]; null = all universal
     const T* Ks;             // per-element matrices, 576 each, row = output DOF
+    int64_t nK;              // matrices held in Ks
     const T* escale;         // finest-level element scale (density extension) or null
     const T* diag;           // 3 planes
     T omega;

@@ -55,6 +55,7 @@ LevelView<T> view(const Level& L, double omega) {
         v.diag = L.diag32.as<T>();
     }
     v.omega = (T)omega;
+    v.nK = v.Ks ? L.nK : 0;
     return v;
 }
 template LevelView<double> view<double>(const Level&, double);
@@ -76,7 +77,8 @@ __device__ __forceinline__ void elem_rows_const(const MatCoef<Tc>& cf, const Tin
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
         const int64_t ns = es + corner_y(j) + corner_x(j) * sx + corner_z(j) * sz;
-        const Tc x0 = (Tc)x[ns], x1 = (Tc)x[ns + S], x2 = (Tc)x[ns + 2 * S];
+        const Tc x0 = (Tc)chk::ld(x, ns, 3 * S, chk::MV_X), x1 = (Tc)chk::ld(x, ns + S, 3 * S, chk::MV_X),
+                 x2 = (Tc)chk::ld(x, ns + 2 * S, 3 * S, chk::MV_X);
         b0 += cf.K[(3 * C + 0) * 24 + 3 * j + 0] * x0 + cf.K[(3 * C + 0) * 24 + 3 * j + 1] * x1 +
               cf.K[(3 * C + 0) * 24 + 3 * j + 2] * x2;
         b1 += cf.K[(3 * C + 1) * 24 + 3 * j + 0] * x0 + cf.K[(3 * C + 1) * 24 + 3 * j + 1] * x1 +
@@ -95,7 +97,8 @@ __device__ __forceinline__ void elem_rows_mat(const Tin* __restrict__ x, int64_t
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
         const int64_t ns = es + corner_y(j) + corner_x(j) * sx + corner_z(j) * sz;
-        const Tc x0 = (Tc)x[ns], x1 = (Tc)x[ns + S], x2 = (Tc)x[ns + 2 * S];
+        const Tc x0 = (Tc)chk::ld(x, ns, 3 * S, chk::MV_X), x1 = (Tc)chk::ld(x, ns + S, 3 * S, chk::MV_X),
+                 x2 = (Tc)chk::ld(x, ns + 2 * S, 3 * S, chk::MV_X);
         a0 += k0[3 * j] * x0 + k0[3 * j + 1] * x1 + k0[3 * j + 2] * x2;
         a1 += k0[24 + 3 * j] * x0 + k0[24 + 3 * j + 1] * x1 + k0[24 + 3 * j + 2] * x2;
         a2 += k0[48 + 3 * j] * x0 + k0[48 + 3 * j + 1] * x1 + k0[48 + 3 * j + 2] * x2;
@@ -110,16 +113,17 @@ __device__ __forceinline__ void elem_contrib(const LevelView<Tc>& lv, const MatC
     constexpr int A = E & 1, B = (E >> 1) & 1, Cz = E >> 2;
     constexpr int C = corner_of(A, B, Cz);     // node = element origin + (A, B, Cz)
     const int64_t es = n - A - B * sx - Cz * sz;
-    if (!lv.emask[es]) return;
+    if (!chk::ld(lv.emask, es, S, chk::MV_ELEM)) return;
     if (lv.etype) {
-        const int t = lv.etype[es];
+        const int t = chk::ld(lv.etype, es, S, chk::MV_ELEM);
         if (t > 0) {
-            elem_rows_mat<Tc, Tin>(x, es, S, sx, sz, lv.Ks + (int64_t)(t - 1) * KE, C, a0, a1, a2);
+            if (chk::ok(t - 1, lv.nK, chk::MV_ELEM))
+                elem_rows_mat<Tc, Tin>(x, es, S, sx, sz, lv.Ks + (int64_t)(t - 1) * KE, C, a0, a1, a2);
             return;
         }
     }
     Tc s = kscale;
-    if (lv.escale) s *= lv.escale[es];
+    if (lv.escale) s *= chk::ld(lv.escale, es, S, chk::MV_ELEM);
     elem_rows_const<Tc, Tin, C>(cf, x, es, S, sx, sz, s, a0, a1, a2);
 }
 
@@ -131,13 +135,14 @@ __device__ __forceinline__ void interior_pairs(const MatCoef<Tc>& cf, const Tin*
                                                int64_t S, int64_t sx, int64_t sz, Tc& a0, Tc& a1, Tc& a2) {
     Tc acc[3];
 #pragma unroll
-    for (int a = 0; a < 3; ++a) acc[a] = cf.S[13 * 9 + 4 * a] * (Tc)x[n + a * S];   // S(0) is diagonal
+    for (int a = 0; a < 3; ++a) acc[a] = cf.S[13 * 9 + 4 * a] * (Tc)chk::ld(x, n + a * S, 3 * S, chk::MV_X);   // S(0) is diagonal
 #pragma unroll
     for (int k = 14; k < 27; ++k) {
         const int64_t o = st_y(k) + st_x(k) * sx + st_z(k) * sz;
         Tc p[3];
 #pragma unroll
-        for (int b = 0; b < 3; ++b) p[b] = (Tc)x[n + o + b * S] + (Tc)x[n - o + b * S];
+        for (int b = 0; b < 3; ++b)
+            p[b] = (Tc)chk::ld(x, n + o + b * S, 3 * S, chk::MV_X) + (Tc)chk::ld(x, n - o + b * S, 3 * S, chk::MV_X);
 #pragma unroll
         for (int a = 0; a < 3; ++a)
 #pragma unroll
@@ -157,9 +162,9 @@ __device__ __forceinline__ bool complement_ok(const LevelView<Tc>& lv, int64_t n
 #pragma unroll
     for (int e = 0; e < 8; ++e) {
         const int64_t es = n - (e & 1) - ((e >> 1) & 1) * sx - (e >> 2) * sz;
-        if (lv.emask[es]) {
+        if (chk::ld(lv.emask, es, lv.g.slots, chk::MV_ELEM)) {
             ++solid;
-            if (lv.etype && lv.etype[es] > 0) return false;
+            if (lv.etype && chk::ld(lv.etype, es, lv.g.slots, chk::MV_ELEM) > 0) return false;
         }
     }
     return solid >= 6;
@@ -173,7 +178,8 @@ __device__ __noinline__ void elem_rows_rt(const MatCoef<Tc>& cf, const Tin* __re
 #pragma unroll 1
     for (int j = 0; j < 8; ++j) {
         const int64_t ns = es + corner_y(j) + corner_x(j) * sx + corner_z(j) * sz;
-        const Tc x0 = (Tc)x[ns], x1 = (Tc)x[ns + S], x2 = (Tc)x[ns + 2 * S];
+        const Tc x0 = (Tc)chk::ld(x, ns, 3 * S, chk::MV_X), x1 = (Tc)chk::ld(x, ns + S, 3 * S, chk::MV_X),
+                 x2 = (Tc)chk::ld(x, ns + 2 * S, 3 * S, chk::MV_X);
         const Tc* k = cf.K + (3 * c) * 24 + 3 * j;
         b0 += k[0] * x0 + k[1] * x1 + k[2] * x2;
         b1 += k[24] * x0 + k[25] * x1 + k[26] * x2;
@@ -192,7 +198,7 @@ __global__ void __launch_bounds__(128) k_matvec(LevelView<Tc> lv, const __grid_c
     if (iy > g.ny || ix > g.nx) return;
     const int64_t n = g.slot(iy, ix, iz);
     const int64_t S = g.slots, sx = g.sx(), sz = g.sz();
-    const uint8_t f = lv.nflag[n];
+    const uint8_t f = chk::ld(lv.nflag, n, S, chk::MV_ELEM);
     Tc a0 = 0, a1 = 0, a2 = 0;
     if (f & NF_INTERIOR) {
         interior_pairs<Tc, Tin>(cf, x, n, S, sx, sz, a0, a1, a2);
@@ -208,7 +214,7 @@ __global__ void __launch_bounds__(128) k_matvec(LevelView<Tc> lv, const __grid_c
         for (int e = 0; e < 8; ++e) {
             const int A = e & 1, B = (e >> 1) & 1, Cz = e >> 2;
             const int64_t es = n - A - B * sx - Cz * sz;
-            if (lv.emask[es]) continue;
+            if (chk::ld(lv.emask, es, S, chk::MV_ELEM)) continue;
             elem_rows_rt<Tc, Tin>(cf, x, es, S, sx, sz, corner_of(A, B, Cz), -kscale, a0, a1, a2);
         }
     } else if (f & NF_SOLID) {
@@ -224,9 +230,9 @@ __global__ void __launch_bounds__(128) k_matvec(LevelView<Tc> lv, const __grid_c
     if (f & NF_FIX_X) a0 = 0;
     if (f & NF_FIX_Y) a1 = 0;
     if (f & NF_FIX_Z) a2 = 0;
-    y[n] = (Tout)a0;
-    y[n + S] = (Tout)a1;
-    y[n + 2 * S] = (Tout)a2;
+    chk::st(y, n, 3 * S, chk::MV_Y, a0);
+    chk::st(y, n + S, 3 * S, chk::MV_Y, a1);
+    chk::st(y, n + 2 * S, 3 * S, chk::MV_Y, a2);
 }
 
 static dim3 node_grid(const Grid& g, dim3 blk) {
@@ -342,27 +348,30 @@ __global__ void k_restrict(Grid gf, Grid gc, const uint8_t* __restrict__ nflag_c
     if (Iy > gc.ny || Ix > gc.nx) return;
     const int64_t cs = gc.slot(Iy, Ix, Iz);
     const int64_t Sf = gf.slots, Sc = gc.slots, sx = gf.sx(), sz = gf.sz();
-    if (!(nflag_c[cs] & NF_SOLID)) {
-        rc[cs] = 0; rc[cs + Sc] = 0; rc[cs + 2 * Sc] = 0;
+    constexpr int R = chk::RESTRICT;
+    if (!(chk::ld(nflag_c, cs, Sc, R) & NF_SOLID)) {
+        chk::st(rc, cs, 3 * Sc, R, 0);
+        chk::st(rc, cs + Sc, 3 * Sc, R, 0);
+        chk::st(rc, cs + 2 * Sc, 3 * Sc, R, 0);
         return;
     }
     const int64_t f0 = gf.slot(2 * Iy, 2 * Ix, 2 * Iz);
 #pragma unroll
     for (int comp = 0; comp < 3; ++comp) {
-        const T* r = rf + comp * Sf;
         T accz = 0;
 #pragma unroll
         for (int c = -1; c <= 1; ++c) {
             T accx = 0;
 #pragma unroll
             for (int b = -1; b <= 1; ++b) {
-                const int64_t s = f0 + b * sx + c * sz;
-                const T line = (T)0.5 * r[s - 1] + r[s] + (T)0.5 * r[s + 1];
+                const int64_t s = comp * Sf + f0 + b * sx + c * sz;
+                const T line = (T)0.5 * chk::ld(rf, s - 1, 3 * Sf, R) + chk::ld(rf, s, 3 * Sf, R) +
+                               (T)0.5 * chk::ld(rf, s + 1, 3 * Sf, R);
                 accx += (b == 0 ? (T)1 : (T)0.5) * line;
             }
             accz += (c == 0 ? (T)1 : (T)0.5) * accx;
         }
-        rc[cs + comp * Sc] = accz;
+        chk::st(rc, cs + comp * Sc, 3 * Sc, R, accz);
     }
 }
 
@@ -385,9 +394,12 @@ __global__ void k_prolong_post(Grid gf, Grid gc, const uint8_t* __restrict__ nfl
     if (iy > gf.ny || ix > gf.nx) return;
     const int64_t fs = gf.slot(iy, ix, iz);
     const int64_t Sf = gf.slots, Sc = gc.slots;
-    const uint8_t fl = nflag_f[fs];
+    constexpr int P = chk::PROLONG;
+    const uint8_t fl = chk::ld(nflag_f, fs, Sf, P);
     if (!(fl & NF_SOLID)) {
-        xf[fs] = 0; xf[fs + Sf] = 0; xf[fs + 2 * Sf] = 0;
+        chk::st(xf, fs, 3 * Sf, P, 0);
+        chk::st(xf, fs + Sf, 3 * Sf, P, 0);
+        chk::st(xf, fs + 2 * Sf, 3 * Sf, P, 0);
         return;
     }
     const int Iy = iy >> 1, Ix = ix >> 1, Iz = iz >> 1;
@@ -397,17 +409,16 @@ __global__ void k_prolong_post(Grid gf, Grid gc, const uint8_t* __restrict__ nfl
     const T wy = oy ? (T)0.5 : (T)1, wx = ox ? (T)0.5 : (T)1, wz = oz ? (T)0.5 : (T)1;
 #pragma unroll
     for (int comp = 0; comp < 3; ++comp) {
-        const T* x = xc + comp * Sc;
         T v = 0;
         for (int c = 0; c <= oz; ++c)
             for (int b = 0; b <= ox; ++b)
                 for (int a = 0; a <= oy; ++a)
-                    v += wy * wx * wz * x[c0 + a + b * csx + c * csz];
+                    v += wy * wx * wz * chk::ld(xc, comp * Sc + c0 + a + b * csx + c * csz, 3 * Sc, P);
         const int64_t i = fs + comp * Sf;
-        const T dd = d[i];
-        T out = (dx[i] + v) + (dd != (T)0 ? (omega * rp[i]) / dd : (T)0);
+        const T dd = chk::ld(d, i, 3 * Sf, P);
+        T out = (chk::ld(dx, i, 3 * Sf, P) + v) + (dd != (T)0 ? (omega * chk::ld(rp, i, 3 * Sf, P)) / dd : (T)0);
         if (zero_fixed && (fl & (NF_FIX_X << comp))) out = 0;
-        xf[i] = out;
+        chk::st(xf, i, 3 * Sf, P, out);
     }
 }
 

@@ -52,9 +52,9 @@ __global__ void __launch_bounds__(128) k_stress_nodal(Grid g, StressCoef cf, con
     for (int e = 0; e < 8; ++e) {
         const int A = e & 1, B = (e >> 1) & 1, C = e >> 2;
         const int64_t es = s - A - B * sx - C * sz;
-        const bool solid = emask[es] != 0;
+        const bool solid = chk::ld(emask, es, S, chk::STRESS_U) != 0;
         cnt += solid;
-        w[A][B][C] = solid ? (escale ? escale[es] : 1.0) : 0.0;
+        w[A][B][C] = solid ? (escale ? chk::ld(escale, es, S, chk::STRESS_U) : 1.0) : 0.0;
     }
     // per axis: total weight of the elements on the forward (0) and backward (1) side
     double wy[2], wx[2], wz[2];
@@ -67,16 +67,17 @@ __global__ void __launch_bounds__(128) k_stress_nodal(Grid g, StressCoef cf, con
     double gr[3][3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        const double* Uc = U + c * S;
-        const double u0 = Uc[s];
-        gr[c][0] = (wx[0] * (Uc[s + sx] - u0) + wx[1] * (u0 - Uc[s - sx])) * cf.ihx;
-        gr[c][1] = -(wy[0] * (Uc[s + 1] - u0) + wy[1] * (u0 - Uc[s - 1])) * cf.ihy;
-        gr[c][2] = (wz[0] * (Uc[s + sz] - u0) + wz[1] * (u0 - Uc[s - sz])) * cf.ihz;
+        const int64_t b = c * S + s;
+        auto u = [&](int64_t off) { return chk::ld(U, b + off, 3 * S, chk::STRESS_U); };
+        const double u0 = u(0);
+        gr[c][0] = (wx[0] * (u(sx) - u0) + wx[1] * (u0 - u(-sx))) * cf.ihx;
+        gr[c][1] = -(wy[0] * (u(1) - u0) + wy[1] * (u0 - u(-1))) * cf.ihy;
+        gr[c][2] = (wz[0] * (u(sz) - u0) + wz[1] * (u0 - u(-sz))) * cf.ihz;
     }
     double o[6];
     hooke_apply(cf, gr, 1.0 / (double)cnt, o);
 #pragma unroll
-    for (int a = 0; a < 6; ++a) out[6 * i + a] = o[a];
+    for (int a = 0; a < 6; ++a) chk::st(out, 6 * i + a, 6 * nn, chk::STRESS_OUT, o[a]);
 }
 
 // One thread per solid voxel: D B(centre) u_e times the voxel's scale.
@@ -90,10 +91,11 @@ __global__ void __launch_bounds__(128) k_stress_voxel(Grid g, StressCoef cf, con
     double gr[3][3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        const double* Uc = U + c * S + es;
         double u[2][2][2];    // [y][x][z] offsets
 #pragma unroll
-        for (int j = 0; j < 8; ++j) u[j & 1][(j >> 1) & 1][j >> 2] = Uc[(j & 1) + ((j >> 1) & 1) * sx + (j >> 2) * sz];
+        for (int j = 0; j < 8; ++j)
+            u[j & 1][(j >> 1) & 1][j >> 2] =
+                chk::ld(U, c * S + es + (j & 1) + ((j >> 1) & 1) * sx + (j >> 2) * sz, 3 * S, chk::STRESS_U);
         const double dx = ((u[0][1][0] - u[0][0][0]) + (u[1][1][0] - u[1][0][0])) +
                           ((u[0][1][1] - u[0][0][1]) + (u[1][1][1] - u[1][0][1]));
         const double dy = ((u[1][0][0] - u[0][0][0]) + (u[1][1][0] - u[0][1][0])) +
@@ -105,9 +107,9 @@ __global__ void __launch_bounds__(128) k_stress_voxel(Grid g, StressCoef cf, con
         gr[c][2] = 0.25 * dz * cf.ihz;
     }
     double o[6];
-    hooke_apply(cf, gr, escale ? escale[es] : 1.0, o);
+    hooke_apply(cf, gr, escale ? chk::ld(escale, es, S, chk::STRESS_U) : 1.0, o);
 #pragma unroll
-    for (int a = 0; a < 6; ++a) out[6 * e + a] = (float)o[a];
+    for (int a = 0; a < 6; ++a) chk::st(out, 6 * e + a, 6 * ne, chk::STRESS_OUT, (float)o[a]);
 }
 
 void stress_dev(Model& M, const double* U, double* nodal, float* per_voxel) {
@@ -145,8 +147,11 @@ __global__ void __launch_bounds__(128) k_grad(Grid g, const int32_t* __restrict_
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
         const int64_t ns = es + corner_y(j) + corner_x(j) * sx + corner_z(j) * sz;
-        u[3 * j] = U[ns]; u[3 * j + 1] = U[ns + S]; u[3 * j + 2] = U[ns + 2 * S];
-        l[3 * j] = Lam[ns]; l[3 * j + 1] = Lam[ns + S]; l[3 * j + 2] = Lam[ns + 2 * S];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            u[3 * j + c] = chk::ld(U, ns + c * S, 3 * S, chk::GRAD);
+            l[3 * j + c] = chk::ld(Lam, ns + c * S, 3 * S, chk::GRAD);
+        }
     }
     // ke_rows[r][c] = Ke0(c, r)
     double en = 0;

@@ -14,7 +14,7 @@
 
 namespace gmgs {
 
-enum { SC_RZ0 = 0, SC_RZ1 = 1, SC_PQ = 2, SC_RR = 3, SC_BB = 4, SC_N = 8 };
+enum { SC_RZ0 = 0, SC_RZ1 = 1, SC_PQ = 2, SC_RR = 3, SC_BB = 4, SC_TC = 5, SC_N = 8 };   // SC_TC: host copy of the tensor-core error flag
 
 static void zalloc(Ctx& c, DevBuf& b, size_t bytes) {
     if (b.bytes < bytes) b = dalloc(bytes);
@@ -179,6 +179,7 @@ static FineLevel fine_level(const Level& lv) {
     f.emask8 = lv.emask8.as<uint8_t>();
     f.etype = lv.etype.as<int32_t>();
     f.Ks = lv.Ks32.as<float>();
+    f.nK = lv.Ks32.p ? lv.nK : 0;
     f.escale = lv.escale32.as<float>();
     f.kscale = (float)lv.kscale;
     f.tile_occ = lv.tile_occ.as<uint8_t>();
@@ -429,7 +430,10 @@ static int pcg_mixed(Model& M, const double* b, double* x, int32_t* iters_out, d
         c.mark(PK_CG_ITER, true);
         GMGS_CUDA(cudaMemcpyAsync(M.scal_host + SC_RR, scal + SC_RR, sizeof(double), cudaMemcpyDeviceToHost,
                                   c.stream));
+        if (M.use_tc)
+            GMGS_CUDA(cudaMemcpyAsync(M.scal_host + SC_TC, M.tc_err.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
         GMGS_CUDA(cudaStreamSynchronize(c.stream));
+        if (M.use_tc && *reinterpret_cast<const int*>(M.scal_host + SC_TC)) break;   // check_tc reports it
         resnorm = std::sqrt(M.scal_host[SC_RR]) / normB;
         if (M.prm.verbose) std::printf(" It.: %4d Res.: %16.6e\n", its, resnorm);
         if (!std::isfinite(resnorm)) {

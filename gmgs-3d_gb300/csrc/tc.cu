@@ -98,6 +98,8 @@ __global__ void __launch_bounds__(NTHR, 4) k_tc_vdown(FineLevel L, const __grid_
             any |= L.tile_occ[((int64_t)iz * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x];
         if (!any) return;
     }
+    // an earlier CTA's tensor-core wait ran out: the result is void, leave at once
+    if (*reinterpret_cast<volatile int*>(err)) return;
     const int t = threadIdx.x, w = t >> 5, lane = t & 31;
 
     for (int i = t; i < B_FLOATS; i += NTHR) Bs[i] = cf.B[i];
@@ -135,23 +137,26 @@ __global__ void __launch_bounds__(NTHR, 4) k_tc_vdown(FineLevel L, const __grid_
             v0[c] = 0.f;
             v1[c] = 0.f;
         }
+        const long long n3 = 3ll * S;
+        constexpr int F = chk::TC_FIELD;
         if (zok && ok0) {
             const int i = base0 + iz * sz;
 #pragma unroll
-            for (int c = 0; c < 3; ++c) v0[c] = r32[i + c * S] * wdinv[i + c * S];
+            for (int c = 0; c < 3; ++c) v0[c] = chk::ld(r32, i + c * S, n3, F) * chk::ld(wdinv, i + c * S, n3, F);
         }
         if (zok && ok1) {
             const int i = base1 + iz * sz;
 #pragma unroll
-            for (int c = 0; c < 3; ++c) v1[c] = r32[i + c * S] * wdinv[i + c * S];
+            for (int c = 0; c < 3; ++c) v1[c] = chk::ld(r32, i + c * S, n3, F) * chk::ld(wdinv, i + c * S, n3, F);
         }
     };
     auto store = [&](int iz, const float (&v0)[3], const float (&v1)[3]) {
-        float* rs = ring + ring_slot(iz) * 3 * SPL;
+        const int rs = ring_slot(iz) * 3 * SPL;
+        constexpr long long R = 3 * 3 * SPL;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            rs[c * SPL + t] = v0[c];
-            if (has_p1) rs[c * SPL + t + NTHR] = v1[c];
+            chk::st(ring, rs + c * SPL + t, R, chk::TC_RING, v0[c]);
+            if (has_p1) chk::st(ring, rs + c * SPL + t + NTHR, R, chk::TC_RING, v1[c]);
         }
     };
 
@@ -162,9 +167,10 @@ __global__ void __launch_bounds__(NTHR, 4) k_tc_vdown(FineLevel L, const __grid_
     auto elem_scale = [&](int ez) -> float {   // 0 for void / foreign-matrix elements
         if (!ecol || ez < 0 || ez >= g.nz) return 0.f;
         const int es = eslot0 + ez * sz;
-        if (!L.emask[es]) return 0.f;
-        if (L.etype && L.etype[es] > 0) return 0.f;
-        return L.escale ? L.escale[es] : 1.f;
+        constexpr int E = chk::TC_ELEM;
+        if (!chk::ld(L.emask, es, S, E)) return 0.f;
+        if (L.etype && chk::ld(L.etype, es, S, E) > 0) return 0.f;
+        return L.escale ? chk::ld(L.escale, es, S, E) : 1.f;
     };
 
     // this thread's owned node (lane, w) for lane < 31, w < 7
@@ -195,7 +201,9 @@ __global__ void __launch_bounds__(NTHR, 4) k_tc_vdown(FineLevel L, const __grid_
             const float* P1 = ring + ring_slot(ez + 1) * 3 * SPL;
             const int o = lane + w * SY;    // staged index of the element's origin node (dy = dx = 0)
             const float s = esc;
-            const float u[3] = {P0[o], P0[SPL + o], P0[2 * SPL + o]};
+            constexpr long long R = 3 * SPL;
+            const float u[3] = {chk::ld(P0, o, R, chk::TC_RING), chk::ld(P0, SPL + o, R, chk::TC_RING),
+                                chk::ld(P0, 2 * SPL + o, R, chk::TC_RING)};
             // column k = 3 j + b of the A row: component b of local node j, in
             // chunks of 8 columns (one tensor-memory store each)
 #pragma unroll
@@ -205,7 +213,7 @@ __global__ void __launch_bounds__(NTHR, 4) k_tc_vdown(FineLevel L, const __grid_
                 for (int i = 0; i < 8; ++i) {
                     const int k = 8 * kk + i, j = k / 3, b = k % 3;
                     const float* P = corner_z(j) ? P1 : P0;
-                    a8[i] = (P[b * SPL + o + corner_y(j) + corner_x(j) * SY] - u[b]) * s;
+                    a8[i] = (chk::ld(P, b * SPL + o + corner_y(j) + corner_x(j) * SY, R, chk::TC_RING) - u[b]) * s;
                 }
                 tc::tmem_st8(tb + lane_base + a_col + 8 * kk, a8);
             }
@@ -239,6 +247,7 @@ __global__ void __launch_bounds__(NTHR, 4) k_tc_vdown(FineLevel L, const __grid_
             ok = tc::mbar_wait_bounded(mbar, phase);   // its writes must end before TMEM is freed
         }
         ok = __all_sync(0xffffffffu, ok);               // tcgen05.ld is warp-collective
+        if (t == 0 && *reinterpret_cast<volatile int*>(err)) stop = 1;   // another CTA gave up
         phase ^= 1u;
         tc::fence_after_sync();
         if (ok) {
@@ -253,7 +262,8 @@ __global__ void __launch_bounds__(NTHR, 4) k_tc_vdown(FineLevel L, const __grid_
                 const float y0 = d[(3 * j) / 8][(3 * j) % 8];
                 const float y1 = d[(3 * j + 1) / 8][(3 * j + 1) % 8];
                 const float y2 = d[(3 * j + 2) / 8][(3 * j + 2) % 8];
-                *reinterpret_cast<float4*>(eo + 4 * c) = make_float4(y0, y1, y2, 0.f);
+                if (chk::ok(t * EOS + 4 * c + 3, NTHR * EOS, chk::TC_EOUT))
+                    *reinterpret_cast<float4*>(eo + 4 * c) = make_float4(y0, y1, y2, 0.f);
             }
         }
         tc::fence_before_sync();
@@ -267,9 +277,13 @@ __global__ void __launch_bounds__(NTHR, 4) k_tc_vdown(FineLevel L, const __grid_
             for (int dy = 0; dy < 2; ++dy)
 #pragma unroll
                 for (int dx = 0; dx < 2; ++dx) {
-                    const float* eo = eout + erow00 - (dy + dx * EY) * EOS;
-                    const float4 b = *reinterpret_cast<const float4*>(eo + 4 * (dy + 2 * dx));
-                    const float4 tp = *reinterpret_cast<const float4*>(eo + 4 * (dy + 2 * dx + 4));
+                    const int eb = erow00 - (dy + dx * EY) * EOS;
+                    const float* eo = eout + eb;
+                    float4 b = make_float4(0.f, 0.f, 0.f, 0.f), tp = b;
+                    if (chk::ok(eb, NTHR * EOS - 32, chk::TC_EOUT)) {
+                        b = *reinterpret_cast<const float4*>(eo + 4 * (dy + 2 * dx));
+                        tp = *reinterpret_cast<const float4*>(eo + 4 * (dy + 2 * dx + 4));
+                    }
                     yb[0] += b.x; yb[1] += b.y; yb[2] += b.z;
                     yt[0] += tp.x; yt[1] += tp.y; yt[2] += tp.z;
                 }
@@ -278,16 +292,16 @@ __global__ void __launch_bounds__(NTHR, 4) k_tc_vdown(FineLevel L, const __grid_
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
                     const float y = (nf & (NF_FIX_X << c)) ? 0.f : yb[c] * L.kscale;
-                    out[n + c * S] = rn[c] - y;
+                    chk::st(out, n + c * S, 3ll * S, chk::TC_OUT, rn[c] - y);
                 }
             }
             part[0] = yt[0]; part[1] = yt[1]; part[2] = yt[2];
             // node data of plane ez + 1 for the next layer
             if (ez + 1 < ze && ez + 1 >= 0) {
                 const int n = nslot0 + (ez + 1) * sz;
-                nf = L.nflag[n];
+                nf = chk::ld(L.nflag, n, S, chk::TC_NODE);
 #pragma unroll
-                for (int c = 0; c < 3; ++c) rn[c] = r32[n + c * S];
+                for (int c = 0; c < 3; ++c) rn[c] = chk::ld(r32, n + c * S, 3ll * S, chk::TC_NODE);
             }
         }
         esc = esc_next;

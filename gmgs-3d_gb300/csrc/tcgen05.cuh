@@ -119,13 +119,21 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* mbar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
 // Bounded wait for the phase with the given parity to complete; false when
-// the limit runs out (the caller records an error and stops using the
-// tensor cores).  Each try_wait suspends the thread for a bounded time.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* mbar, uint32_t parity, uint32_t max_tries = 1u << 22) {
-    for (uint32_t i = 0; i < max_tries; ++i)
+// the time limit (default 20 ms; an MMA of these kernels takes microseconds)
+// runs out: the caller records an error and stops using the tensor cores.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* mbar, uint32_t parity, uint64_t limit_ns = 20000000ull) {
+    if (mbar_try_wait(mbar, parity)) return true;
+    const uint64_t t0 = globaltimer_ns();
+    for (;;) {
         if (mbar_try_wait(mbar, parity)) return true;
-    return false;
+        if (globaltimer_ns() - t0 > limit_ns) return false;
+    }
 }
 
 }  // namespace tc

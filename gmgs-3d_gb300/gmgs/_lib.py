@@ -9,7 +9,9 @@ import ctypes as C
 import os
 from pathlib import Path
 
-LIB_PATH = Path(__file__).resolve().parent / "libgmgs.so"
+# GMGS_LIB selects another build of the library, e.g. the checked build
+# (gmgs-3d_gb300/build.py --debug writes libgmgs_checked.so)
+LIB_PATH = Path(os.environ.get("GMGS_LIB") or Path(__file__).resolve().parent / "libgmgs.so")
 
 # status codes (enum gmgs_status)
 OK = 0

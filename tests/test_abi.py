@@ -89,3 +89,17 @@ def test_missing_library_fails_loudly(tmp_path):
     from gmgs import _lib
     with pytest.raises(_lib.GMGSLibraryMissing):
         _lib.load(tmp_path / "libgmgs.so")
+
+
+def test_checked_build_compiles_and_exports_every_symbol():
+    """build.py --debug (GMGS_CHECKED) compiles on its own objects into
+    libgmgs_checked.so, which exports the same C ABI."""
+    import sys
+    sys.path.insert(0, str(ROOT / "gmgs-3d_gb300"))
+    import build as B
+    path = B.build(debug=True)
+    assert path.name == "libgmgs_checked.so" and path != B.LIB
+    from gmgs import _lib
+    chk = _lib.load(path)
+    for name in declared_functions():
+        assert hasattr(chk, name), name

@@ -34,7 +34,7 @@ def rel(a, b):
 
 cases = [("ragged_L3", synthetic.sphere_voids(21, 13, 18, 6, 7), 3, None),
          ("block42_L5", synthetic.make("block42_fp64")[0], 5, None),
-         ("density_L3", synthetic.sphere_voids(24, 20, 28, 4, 3), 3, (0.3, 1.0))]
+         ("density_L3", synthetic.sphere_voids(28, 24, 32, 2, 5), 3, (0.3, 1.0))]
 for name, vox, L, rr in cases:
     fixed, loads = synthetic.boundary_conditions(vox, L)
     rho = synthetic.density(int(vox.sum()), rr, 5) if rr else None

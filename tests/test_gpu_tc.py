@@ -22,7 +22,7 @@ CASES = {
     # levels 3-4 store one Galerkin matrix per element: their nodes go to the per-element kernel
     "block42_L5": (lambda: synthetic.make("block42_fp64")[0], 5, None),
     # finest-level element scales: every level below holds per-element matrices
-    "density_L3": (lambda: synthetic.sphere_voids(24, 20, 28, 4, 3), 3, (0.3, 1.0)),
+    "density_L3": (lambda: synthetic.sphere_voids(28, 24, 32, 2, 5), 3, (0.3, 1.0)),
 }
 
 

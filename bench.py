@@ -538,7 +538,7 @@ def run_gmgs(a):
                      "frac": achieved / hbm if achieved else None,
                      "traffic": UJ_TRAFFIC_PER_NODE * nn if UJ_TRAFFIC_PER_NODE else None,
                      "kernel": "k_fine<FM_CG_UPDATE_JACOBI> (finest CG update + Jacobi step + K dx)",
-                     "algorithmic_bytes_per_node": 158, "launches_timed": nl,
+                     "algorithmic_bytes_per_node": (mv_bytes / max(nl, 1) / nn) if nl else None, "launches_timed": nl,
                      "ms_per_launch": mv_ms / max(nl, 1), "peak_source": peak_note},
         "gpu_launches": launches,
         "breakdown": breakdown,

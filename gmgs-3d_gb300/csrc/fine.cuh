@@ -24,7 +24,15 @@ struct FineLevel {
     const float* escale;     // finest-level element scale or null
     float kscale;
     const uint8_t* tile_occ; // per (z plane, x tile, y tile) of the streaming kernel: any solid node; null = all
+    // Uniform level (no per-element matrix or scale): omega / diag of a node
+    // depends only on which of its 8 elements are solid, so wtab[3 * emask8 + a]
+    // replaces the wdinv vector's 12 bytes per node (null: read wdinv).
+    const float* wtab;
 };
+constexpr int WTAB_FLOATS = 256 * 3;
+// omega / diag for every 8-element mask of a uniform level, summed in the
+// order of the diagonal kernel so that every entry equals the wdinv vector's
+void make_wtab(const double* ke_rows, double kscale, double omega, float* wtab);
 
 struct DotOut {
     double* partials = nullptr;   // one per block
@@ -256,8 +264,8 @@ template <int MODE>
 void launch_fine(Ctx& c, const FineLevel& L, const Coef32& cf, const FineArgs& a);
 
 void launch_up32(Ctx& c, const Grid& gf, const Grid& gc, const uint8_t* nflag, const uint8_t* tile_occ,
-                 const float* wdinv, const float* r, const float* rp, const float* xc, float* xf, bool zero_fixed,
-                 const DotOut* dot);
+                 const float* wdinv, const uint8_t* emask8, const float* wtab, const float* r, const float* rp,
+                 const float* xc, float* xf, bool zero_fixed, const DotOut* dot);
 void launch_wdinv(Ctx& c, int64_t n, const double* d, double omega, float* w);
 void launch_perel_vdown(Ctx& c, const FineLevel& L, const Coef32& cf, const int32_t* nodes, int count, const float* r,
                         const float* w, float* out);

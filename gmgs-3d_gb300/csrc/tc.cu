@@ -49,9 +49,9 @@ constexpr int EOS = 36;                   // floats per element in the output bu
 constexpr int TC_COLS = 128;              // tensor-memory columns per CTA: A and D of two MMA groups
 constexpr int B_FLOATS = 32 * 24;
 constexpr int RING_FLOATS = (3 * 3 * SPL + 3) / 4 * 4;   // 2,676 floats: the next buffer stays 16-byte aligned
-constexpr size_t SMEM_BYTES = (size_t)(B_FLOATS + RING_FLOATS + NTHR * EOS) * 4 + 16;   // + mbarrier, TMEM address, stop flag
-static_assert((B_FLOATS + RING_FLOATS) % 4 == 0, "element-output buffer must be 16-byte aligned");
-static_assert((B_FLOATS + RING_FLOATS + NTHR * EOS) % 2 == 0, "the mbarrier must be 8-byte aligned");
+constexpr size_t SMEM_BYTES = (size_t)(B_FLOATS + WTAB_FLOATS + RING_FLOATS + NTHR * EOS) * 4 + 16;   // + mbarrier, TMEM address, stop flag
+static_assert((B_FLOATS + WTAB_FLOATS + RING_FLOATS) % 4 == 0, "element-output buffer must be 16-byte aligned");
+static_assert((B_FLOATS + WTAB_FLOATS + RING_FLOATS + NTHR * EOS) % 2 == 0, "the mbarrier must be 8-byte aligned");
 constexpr uint32_t IDESC = tc::idesc_tf32(128, 32);
 
 __device__ __forceinline__ int ring_slot(int z) { return (z + 3) % 3; }   // z >= -1
@@ -79,7 +79,8 @@ __global__ void __launch_bounds__(NTHR, 4) k_tc_vdown(FineLevel L, const __grid_
                                                      float* __restrict__ out, int zc, int* __restrict__ err) {
     extern __shared__ __align__(16) float smem[];
     float* Bs = smem;
-    float* ring = Bs + B_FLOATS;
+    float* stab = Bs + B_FLOATS;          // omega / diag by element mask (uniform level) or unused
+    float* ring = stab + WTAB_FLOATS;
     float* eout = ring + RING_FLOATS;
     uint64_t* mbar = reinterpret_cast<uint64_t*>(eout + NTHR * EOS);
     uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
@@ -103,6 +104,9 @@ __global__ void __launch_bounds__(NTHR, 4) k_tc_vdown(FineLevel L, const __grid_
     const int t = threadIdx.x, w = t >> 5, lane = t & 31;
 
     for (int i = t; i < B_FLOATS; i += NTHR) Bs[i] = cf.B[i];
+    const bool wt = L.wtab != nullptr;
+    if (wt)
+        for (int i = t; i < WTAB_FLOATS; i += NTHR) stab[i] = L.wtab[i];
     if (w == 0) {
         tc::tmem_alloc(tslot, TC_COLS);
         tc::tmem_relinquish();
@@ -139,16 +143,14 @@ __global__ void __launch_bounds__(NTHR, 4) k_tc_vdown(FineLevel L, const __grid_
         }
         const long long n3 = 3ll * S;
         constexpr int F = chk::TC_FIELD;
-        if (zok && ok0) {
-            const int i = base0 + iz * sz;
+        auto point = [&](int i, float (&v)[3]) {
+            const int m3 = wt ? 3 * chk::ld(L.emask8, i, S, F) : 0;
 #pragma unroll
-            for (int c = 0; c < 3; ++c) v0[c] = chk::ld(r32, i + c * S, n3, F) * chk::ld(wdinv, i + c * S, n3, F);
-        }
-        if (zok && ok1) {
-            const int i = base1 + iz * sz;
-#pragma unroll
-            for (int c = 0; c < 3; ++c) v1[c] = chk::ld(r32, i + c * S, n3, F) * chk::ld(wdinv, i + c * S, n3, F);
-        }
+            for (int c = 0; c < 3; ++c)
+                v[c] = chk::ld(r32, i + c * S, n3, F) * (wt ? stab[m3 + c] : chk::ld(wdinv, i + c * S, n3, F));
+        };
+        if (zok && ok0) point(base0 + iz * sz, v0);
+        if (zok && ok1) point(base1 + iz * sz, v1);
     };
     auto store = [&](int iz, const float (&v0)[3], const float (&v1)[3]) {
         const int rs = ring_slot(iz) * 3 * SPL;

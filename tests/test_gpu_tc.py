@@ -5,8 +5,8 @@ and against the oracle.
 The tensor cores read the down-sweep's element differences as TF32 (10-bit
 mantissa).  That only changes the preconditioner: the preconditioned residual
 agrees with the FP32 kernels' and the oracle's to TF32 accuracy, and the
-mixed solve reaches the same tolerance in the same number of iterations (one
-more at most) with the displacement within 1e-5 of the FP64 oracle.
+mixed solve reaches the same tolerance within one iteration of the oracle's
+count, with the displacement within 1e-5 of the FP64 oracle.
 """
 import numpy as np
 import pytest
@@ -83,7 +83,26 @@ def test_tc_mixed_solve_matches_oracle(name, monkeypatch):
     monkeypatch.setenv("GMGS_TC", "1")
     s = _solver(vox, fixed, loads, L, rho)
     u = s.solve()
-    assert s.status == 0
-    assert o.iterations <= s.iterations <= o.iterations + 1
+    assert s.status == 0 and s.relres < 1e-3
+    assert abs(s.iterations - o.iterations) <= 1
     assert rel(u, u_ref) < 1e-5
     s.close()
+
+
+@pytest.mark.parametrize("tc", ["0", "1"])
+def test_diagonal_table_is_bit_identical(tc, monkeypatch):
+    """On a uniform finest level the kernels take omega / diag from a table
+    indexed by the node's 8-element mask instead of the wdinv vector; the
+    table is summed like the diagonal kernel, so the mixed solve is bitwise
+    the same with and without it (GMGS_WTAB=0)."""
+    vox, fixed, loads, L, _ = _inputs("block42_L4")
+    monkeypatch.setenv("GMGS_TC", tc)
+    out = {}
+    for wt in ("1", "0"):
+        monkeypatch.setenv("GMGS_WTAB", wt)
+        s = Solver(vox, omega=0.4, num_levels=L, precision="mixed")
+        s.set_bc(fixed, loads)
+        out[wt] = (s.solve(), s.iterations)
+        s.close()
+    assert out["1"][1] == out["0"][1]
+    assert np.array_equal(out["1"][0], out["0"][0])

@@ -278,10 +278,12 @@ __global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? 3 : 5)
                         rinc = fmaf(alpha, ed.q[b], rinc);
                         rm32 = fmaf(-alpha, ed.q[b], rm32);
                     }
-                    chk::st(a.x64, i, n3, O, ed.x64[b] + (double)xinc);
-                    const double rn = ed.r64[b] - (double)rinc;
+                    const double xd = a.icvt ? f2d_int(xinc) : (double)xinc;
+                    const double rd = a.icvt ? f2d_int(rinc) : (double)rinc;
+                    chk::st(a.x64, i, n3, O, ed.x64[b] + xd);
+                    const double rn = ed.r64[b] - rd;
                     chk::st(a.r64, i, n3, O, rn);
-                    chk::st(a.r32out, i, n3, O, (float)rn);
+                    chk::st(a.r32out, i, n3, O, a.icvt == 2 ? d2f_int(rn) : (float)rn);
                     dot.add(rm32 * rm32);
                 } else {
                     chk::st(a.pout, i, n3, O, v);

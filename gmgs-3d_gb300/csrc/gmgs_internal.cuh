@@ -84,13 +84,13 @@ __device__ __forceinline__ bool ok(long long i, long long n, int site) {
     atomicCAS(&g_first, 0ull, ((unsigned long long)site << 48) | ((unsigned long long)i & 0xFFFFFFFFFFFFull));
     return false;
 }
-template <typename T>
-__device__ __forceinline__ T ld(const T* p, long long i, long long n, int site) {
-    return ok(i, n, site) ? p[i] : T(0);
+template <typename T, typename I>
+__device__ __forceinline__ T ld(const T* p, I i, long long n, int site) {
+    return ok((long long)i, n, site) ? p[i] : T(0);
 }
-template <typename T, typename V>
-__device__ __forceinline__ void st(T* p, long long i, long long n, int site, V v) {
-    if (ok(i, n, site)) p[i] = (T)v;
+template <typename T, typename I, typename V>
+__device__ __forceinline__ void st(T* p, I i, long long n, int site, V v) {
+    if (ok((long long)i, n, site)) p[i] = (T)v;
 }
 // host: each translation unit registers a reader of its own device words
 using Reader = bool (*)(std::string& msg);
@@ -118,11 +118,12 @@ static bool read_this_unit(std::string& msg) {
 }
 static const bool g_reader_added = (add_reader(&read_this_unit), true);
 #else
+// the index keeps the caller's type: 32-bit indices stay 32-bit address arithmetic
 __device__ __forceinline__ bool ok(long long, long long, int) { return true; }
-template <typename T>
-__device__ __forceinline__ T ld(const T* p, long long i, long long, int) { return p[i]; }
-template <typename T, typename V>
-__device__ __forceinline__ void st(T* p, long long i, long long, int, V v) { p[i] = (T)v; }
+template <typename T, typename I>
+__device__ __forceinline__ T ld(const T* p, I i, long long, int) { return p[i]; }
+template <typename T, typename I, typename V>
+__device__ __forceinline__ void st(T* p, I i, long long, int, V v) { p[i] = (T)v; }
 #endif
 }  // namespace chk
 

@@ -356,6 +356,8 @@ static int pcg_mixed(Model& M, const double* b, double* x, int32_t* iters_out, d
     // (omega / diag comes from the element mask, already counted with the flags, when the level has the table)
     const double jbytes = (double)l0.n_node * 3 * (16 + 8 + 4 + 4 + (l0.wtab.p ? 0 : 4) + 16) + 2.0 * (double)l0.n_node;
     const double pbytes = (double)l0.n_node * 3 * (4 + 4 + 4 + 4) + 2.0 * (double)l0.n_node;
+    const char* icvt_env = std::getenv("GMGS_INTCVT");
+    const int icvt = icvt_env ? std::atoi(icvt_env) : 0;
 
     // Fused kernel: the previous iteration's update (x += alpha p, r -= alpha q,
     // |r|^2 for its convergence test) followed by the next iteration's Jacobi
@@ -373,6 +375,7 @@ static int pcg_mixed(Model& M, const double* b, double* x, int32_t* iters_out, d
         a.scal = scal;
         a.cur = cur;
         a.first = first;
+        a.icvt = icvt;
         a.dot = dot_out(M, SC_RR);
         c.mark(PK_FINE_MATVEC, false);
         c.mark(PK_UPDATE_JACOBI, false);

@@ -62,49 +62,25 @@ void make_stencil(const double* ke_rows, Coef32& cf) {
     for (int i = 0; i < KE; ++i) cf.K[i] = (float)ke_rows[i];
 }
 
-// omega / diag of a node of a uniform level for each mask of its solid
-// elements (bit A + 2B + 4C: the element at node - (A, B, C)): the diagonal
-// kernel's sum, element by element in the same order, of kscale times the
-// corner's diagonal entry of Ke0 (kscale is a power of two, so the product is
-// exact), then the FP64 quotient rounded to FP32 as k_wdinv rounds it
-void make_wtab(const double* ke_rows, double kscale, double omega, float* wtab) {
-    for (int m = 0; m < 256; ++m)
-        for (int a = 0; a < 3; ++a) {
-            double d = 0.0;
-            for (int e = 0; e < 8; ++e) {
-                if (!((m >> e) & 1)) continue;
-                const int c = corner_of(e & 1, (e >> 1) & 1, e >> 2);
-                d += kscale * 1.0 * ke_rows[(3 * c + a) * 24 + 3 * c + a];
-            }
-            wtab[3 * m + a] = d != 0.0 ? (float)(omega / d) : 0.f;
-        }
-}
-
 // ---------------------------------------------------------------------------
 // the fused streaming kernel
 // ---------------------------------------------------------------------------
 // input field at one point (3 components) from the kernel's inputs
-// stab: the level's omega / diag table in shared memory (null: read wdinv)
 template <int MODE>
-__device__ __forceinline__ void field_at(const FineArgs& a, const FineLevel& L, const float* stab, int S, int s,
-                                         float beta, float alpha, float v[3]) {
+__device__ __forceinline__ void field_at(const FineArgs& a, int S, int s, float beta, float alpha, float v[3]) {
     const long long n3 = 3ll * S;
     constexpr int F = chk::FINE_FIELD;
-    int m3 = 0;
-    if ((MODE == FM_VCYCLE_DOWN || MODE == FM_CG_UPDATE_JACOBI) && stab) m3 = 3 * chk::ld(L.emask8, s, S, F);
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         const int i = s + c * S;
         if (MODE == FM_PLAIN) {
             v[c] = chk::ld(a.v, i, n3, F);
         } else if (MODE == FM_VCYCLE_DOWN) {
-            const float w = stab ? stab[m3 + c] : chk::ld(a.wdinv, i, n3, F);
-            v[c] = chk::ld(a.r32, i, n3, F) * w;
+            v[c] = chk::ld(a.r32, i, n3, F) * chk::ld(a.wdinv, i, n3, F);
         } else if (MODE == FM_CG_UPDATE_JACOBI) {
             const float r = chk::ld(a.r32, i, n3, F);
             const float rm = a.first ? r : fmaf(-alpha, chk::ld(a.q32, i, n3, F), r);
-            const float w = stab ? stab[m3 + c] : chk::ld(a.wdinv, i, n3, F);
-            v[c] = rm * w;
+            v[c] = rm * chk::ld(a.wdinv, i, n3, F);
         } else {   // FM_CG_DIRECTION
             const float z = chk::ld(a.z32, i, n3, F);
             v[c] = a.first ? z : fmaf(beta, chk::ld(a.pold, i, n3, F), z);
@@ -150,8 +126,6 @@ __global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? 3 : 5)
     k_fine(FineLevel L, const __grid_constant__ Coef32 cf, FineArgs a, int zc) {
     __shared__ float ring[RING][3 * PLANE];
     __shared__ double sh[32];
-    constexpr bool USES_W = MODE == FM_VCYCLE_DOWN || MODE == FM_CG_UPDATE_JACOBI;
-    __shared__ float stab_s[USES_W ? WTAB_FLOATS : 1];
     const Grid& g = L.g;
     const int S = (int)g.slots;
     const int sz = g.py * g.px;
@@ -171,12 +145,6 @@ __global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? 3 : 5)
     const int tid = threadIdx.x + threadIdx.y * TY;
     const int wrp = tid >> 5, lane = tid & 31;
     const int ly = (wrp & 3) * 8 + (lane & 7), lx = (wrp >> 2) * 4 + (lane >> 3);
-    const float* stab = nullptr;
-    if (USES_W && L.wtab) {
-        for (int i = tid; i < WTAB_FLOATS; i += NT) stab_s[i] = L.wtab[i];
-        __syncthreads();
-        stab = stab_s;
-    }
 
     float beta = 0.f, alpha = 0.f;
     if (MODE == FM_CG_DIRECTION && !a.first) beta = (float)(a.scal[a.cur] / a.scal[a.cur ^ 1]);
@@ -202,8 +170,8 @@ __global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? 3 : 5)
         vc[0] = vc[1] = vc[2] = 0.f;
         vh[0] = vh[1] = vh[2] = 0.f;
         const bool zok = iz >= -1 && iz <= g.nz + 1;
-        if (zok && ccol) field_at<MODE>(a, L, stab, S, cbase + iz * sz, beta, alpha, vc);
-        if (zok && hcol) field_at<MODE>(a, L, stab, S, hbase + iz * sz, beta, alpha, vh);
+        if (zok && ccol) field_at<MODE>(a, S, cbase + iz * sz, beta, alpha, vc);
+        if (zok && hcol) field_at<MODE>(a, S, hbase + iz * sz, beta, alpha, vh);
     };
     auto store = [&](float* r, const float vc[3], const float vh[3]) {
         constexpr long long R = 3 * PLANE;
@@ -278,12 +246,10 @@ __global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? 3 : 5)
                         rinc = fmaf(alpha, ed.q[b], rinc);
                         rm32 = fmaf(-alpha, ed.q[b], rm32);
                     }
-                    const double xd = a.icvt ? f2d_int(xinc) : (double)xinc;
-                    const double rd = a.icvt ? f2d_int(rinc) : (double)rinc;
-                    chk::st(a.x64, i, n3, O, ed.x64[b] + xd);
-                    const double rn = ed.r64[b] - rd;
+                    chk::st(a.x64, i, n3, O, ed.x64[b] + (double)xinc);
+                    const double rn = ed.r64[b] - (double)rinc;
                     chk::st(a.r64, i, n3, O, rn);
-                    chk::st(a.r32out, i, n3, O, a.icvt == 2 ? d2f_int(rn) : (float)rn);
+                    chk::st(a.r32out, i, n3, O, (float)rn);
                     dot.add(rm32 * rm32);
                 } else {
                     chk::st(a.pout, i, n3, O, v);
@@ -340,16 +306,10 @@ template void launch_fine<FM_CG_DIRECTION>(Ctx&, const FineLevel&, const Coef32&
 template <bool DOT>
 __global__ void __launch_bounds__(256, 4) k_up32(Grid gf, Grid gc, const uint8_t* __restrict__ nflag,
                                               const uint8_t* __restrict__ tile_occ, int zc,
-                                              const float* __restrict__ wdinv, const uint8_t* __restrict__ emask8,
-                                              const float* __restrict__ wtab, const float* __restrict__ r,
+                                              const float* __restrict__ wdinv, const float* __restrict__ r,
                                               const float* __restrict__ rp, const float* __restrict__ xc,
                                               float* __restrict__ xf, int zero_fixed, DotOut dout) {
     __shared__ double sh[32];
-    __shared__ float stab[WTAB_FLOATS];
-    if (wtab) {
-        for (int i = threadIdx.x + threadIdx.y * TY; i < WTAB_FLOATS; i += NT) stab[i] = wtab[i];
-        __syncthreads();
-    }
     const int Sf = (int)gf.slots, Sc = (int)gc.slots;
     const int csx = gc.py, csz = gc.py * gc.px, fsz = gf.py * gf.px;
     const int iy = blockIdx.x * TY + threadIdx.x, ix = blockIdx.y * TX + threadIdx.y;
@@ -387,10 +347,9 @@ __global__ void __launch_bounds__(256, 4) k_up32(Grid gf, Grid gc, const uint8_t
             const long long n3f = 3ll * Sf;
             constexpr int U = chk::UP_FINE;
             fl = chk::ld(nflag, fs, Sf, U);
-            const int m3 = wtab ? 3 * chk::ld(emask8, fs, Sf, U) : 0;
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                wd[c] = wtab ? stab[m3 + c] : chk::ld(wdinv, fs + c * Sf, n3f, U);
+                wd[c] = chk::ld(wdinv, fs + c * Sf, n3f, U);
                 rr[c] = chk::ld(r, fs + c * Sf, n3f, U);
                 rq[c] = chk::ld(rp, fs + c * Sf, n3f, U);
             }
@@ -448,17 +407,16 @@ static int up32_zc(const Grid& g, const Ctx& c) {
 }
 
 void launch_up32(Ctx& c, const Grid& gf, const Grid& gc, const uint8_t* nflag, const uint8_t* tile_occ,
-                 const float* wdinv, const uint8_t* emask8, const float* wtab, const float* r, const float* rp,
-                 const float* xc, float* xf, bool zero_fixed, const DotOut* dot) {
+                 const float* wdinv, const float* r, const float* rp, const float* xc, float* xf, bool zero_fixed,
+                 const DotOut* dot) {
     const int zc = up32_zc(gf, c);
     const dim3 grid((gf.ny + 1 + TY - 1) / TY, (gf.nx + 1 + TX - 1) / TX, (gf.nz + 1 + zc - 1) / zc);
     const dim3 blk(TY, TX, 1);
     if (dot) {
-        k_up32<true><<<grid, blk, 0, c.stream>>>(gf, gc, nflag, tile_occ, zc, wdinv, emask8, wtab, r, rp, xc, xf,
-                                                  zero_fixed, *dot);
+        k_up32<true><<<grid, blk, 0, c.stream>>>(gf, gc, nflag, tile_occ, zc, wdinv, r, rp, xc, xf, zero_fixed, *dot);
     } else {
-        k_up32<false><<<grid, blk, 0, c.stream>>>(gf, gc, nflag, tile_occ, zc, wdinv, emask8, wtab, r, rp, xc, xf,
-                                                   zero_fixed, DotOut{});
+        k_up32<false><<<grid, blk, 0, c.stream>>>(gf, gc, nflag, tile_occ, zc, wdinv, r, rp, xc, xf, zero_fixed,
+                                                   DotOut{});
     }
     GMGS_LAUNCHED(c);
 }

@@ -24,15 +24,7 @@ struct FineLevel {
     const float* escale;     // finest-level element scale or null
     float kscale;
     const uint8_t* tile_occ; // per (z plane, x tile, y tile) of the streaming kernel: any solid node; null = all
-    // Uniform level (no per-element matrix or scale): omega / diag of a node
-    // depends only on which of its 8 elements are solid, so wtab[3 * emask8 + a]
-    // replaces the wdinv vector's 12 bytes per node (null: read wdinv).
-    const float* wtab;
 };
-constexpr int WTAB_FLOATS = 256 * 3;
-// omega / diag for every 8-element mask of a uniform level, summed in the
-// order of the diagonal kernel so that every entry equals the wdinv vector's
-void make_wtab(const double* ke_rows, double kscale, double omega, float* wtab);
 
 struct DotOut {
     double* partials = nullptr;   // one per block
@@ -63,7 +55,6 @@ struct FineArgs {
     float* pout = nullptr;           // new direction (must not alias pold)
     double* x64 = nullptr;           // solution (owned nodes, in place)
     float* r32out = nullptr;         // FP32 copy of the updated residual (must not alias r32)
-    int icvt = 0;                    // FM_CG_UPDATE_JACOBI conversions on the integer pipe: 1 float->double, 2 both
     DotOut dot;
 };
 
@@ -76,36 +67,6 @@ __host__ __device__ constexpr int off_comp(int k, int a) { return a == 0 ? off_x
 // structural non-zeros of the assembled interior block S(d)[a][b]
 __host__ __device__ constexpr bool s_nonzero(int k, int a, int b) {
     return a == b || (off_comp(k, a) != 0 && off_comp(k, b) != 0);
-}
-
-// ---------------------------------------------------------------------------
-// FP32 <-> FP64 conversions on the integer pipe.  GB300 runs conversions
-// between float and double on its FP64 pipe, at the rate of DADD (about 2
-// lanes per clock per SM, measured); the CG update needs three per DOF.
-// ---------------------------------------------------------------------------
-// float -> double, exact: the exponent is re-biased and the 23 mantissa bits
-// move to the top of the 52.  Zero, subnormal (|f| < 2^-126), infinite and NaN
-// inputs take the hardware conversion.
-__device__ __forceinline__ double f2d_int(float f) {
-    const uint32_t u = __float_as_uint(f);
-    const uint32_t e = (u >> 23) & 0xFFu;
-    if (e == 0u || e == 0xFFu) return (double)f;
-    const uint32_t hi = (u & 0x80000000u) | (((u & 0x7FFFFFFFu) >> 3) + 0x38000000u);
-    return __hiloint2double((int)hi, (int)(u << 29));
-}
-// double -> float, round to nearest even: the 23 leading mantissa bits, plus
-// one when the dropped 29 bits are above half an ulp, or exactly half with an
-// odd result (a carry out of the mantissa raises the exponent, as it should).
-// Results outside the normal float range (and zero, infinities, NaN) take the
-// hardware conversion.
-__device__ __forceinline__ float d2f_int(double d) {
-    const uint32_t hi = (uint32_t)__double2hiint(d), lo = (uint32_t)__double2loint(d);
-    const uint32_t e = (hi >> 20) & 0x7FFu;
-    if (e < 897u || e > 1150u) return (float)d;
-    uint32_t t = ((e - 896u) << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29);
-    const uint32_t half = (lo >> 28) & 1u, rest = (lo & 0x0FFFFFFFu) != 0u;
-    t += half & (rest | (t & 1u));
-    return __uint_as_float((hi & 0x80000000u) | t);
 }
 
 // ---------------------------------------------------------------------------
@@ -295,8 +256,8 @@ template <int MODE>
 void launch_fine(Ctx& c, const FineLevel& L, const Coef32& cf, const FineArgs& a);
 
 void launch_up32(Ctx& c, const Grid& gf, const Grid& gc, const uint8_t* nflag, const uint8_t* tile_occ,
-                 const float* wdinv, const uint8_t* emask8, const float* wtab, const float* r, const float* rp,
-                 const float* xc, float* xf, bool zero_fixed, const DotOut* dot);
+                 const float* wdinv, const float* r, const float* rp, const float* xc, float* xf, bool zero_fixed,
+                 const DotOut* dot);
 void launch_wdinv(Ctx& c, int64_t n, const double* d, double omega, float* w);
 void launch_perel_vdown(Ctx& c, const FineLevel& L, const Coef32& cf, const int32_t* nodes, int count, const float* r,
                         const float* w, float* out);

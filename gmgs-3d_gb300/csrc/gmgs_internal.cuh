@@ -238,7 +238,6 @@ struct Level {
     DevBuf vr, vrp, vdx, vx, vy;
     DevBuf tile_occ;          // mixed path: per 32x8 node tile and z plane, 1 if it holds a solid node
     DevBuf wdinv32;           // mixed path: omega / diag in FP32
-    DevBuf wtab;              // mixed path, uniform finest level: omega / diag by 8-element mask (256 x 3 FP32)
     DevBuf emask8;            // mixed path: per-node mask of the 8 surrounding solid elements
     DevBuf perel_nodes;       // slots of nodes touching an element with its own stored matrix
     DevBuf tc_occ;            // mixed path: per 31x7 node tile (tensor-core kernels) and z plane, 1 if solid

@@ -57,17 +57,6 @@ void alloc_work(Model& M) {
                 launch_tile_occ(c, lv.g, lv.nflag.as<uint8_t>(), lv.tile_occ.as<uint8_t>());
                 if (lv.tc_occ.bytes < tc_tile_occ_bytes(lv.g)) lv.tc_occ = dalloc(tc_tile_occ_bytes(lv.g));
                 launch_tc_tile_occ(c, lv.g, lv.nflag.as<uint8_t>(), lv.tc_occ.as<uint8_t>());
-                // uniform finest level: omega / diag from the node's element mask
-                // (environment GMGS_WTAB=0 reads the wdinv vector instead)
-                const char* wt_env = std::getenv("GMGS_WTAB");
-                if (l == 0 && !lv.escale64.p && !lv.etype.p && !(wt_env && wt_env[0] == '0')) {
-                    std::vector<float> t(WTAB_FLOATS);
-                    make_wtab(M.ke0_rows, lv.kscale, M.prm.omega, t.data());
-                    if (lv.wtab.bytes < WTAB_FLOATS * sizeof(float)) lv.wtab = dalloc(WTAB_FLOATS * sizeof(float));
-                    GMGS_CUDA(cudaMemcpy(lv.wtab.p, t.data(), WTAB_FLOATS * sizeof(float), cudaMemcpyHostToDevice));
-                } else {
-                    lv.wtab = DevBuf();
-                }
             }
         }
     }
@@ -194,7 +183,6 @@ static FineLevel fine_level(const Level& lv) {
     f.escale = lv.escale32.as<float>();
     f.kscale = (float)lv.kscale;
     f.tile_occ = lv.tile_occ.as<uint8_t>();
-    f.wtab = lv.wtab.as<float>();
     return f;
 }
 
@@ -223,8 +211,8 @@ static void vcycle32(Model& M, const float* r32, float* z, bool with_dot, int do
         a.r32 = l == 0 ? r32 : lv.vr.as<float>();
         a.wdinv = lv.wdinv32.as<float>();
         a.out32 = lv.vrp.as<float>();
-        // r, omega/diag (or the 1-byte element mask with the table), r' per node; element masks
-        const double bytes = (double)lv.n_node * (lv.wtab.p ? 3 * 8 + 1 : 3 * 12) + (double)lv.n_elem;
+        // r, omega/diag, r' per node; element masks
+        const double bytes = (double)lv.n_node * 3 * 12 + (double)lv.n_elem;
         if (l == 0) {
             c.mark(PK_FINE_MATVEC, false);
             c.mark(PK_VDOWN0, false);
@@ -262,10 +250,10 @@ static void vcycle32(Model& M, const float* r32, float* z, bool with_dot, int do
             c.mark(PK_UP0, false);
         }
         launch_up32(c, lv.g, M.levels[l + 1].g, lv.nflag.as<uint8_t>(), lv.tile_occ.as<uint8_t>(),
-                    lv.wdinv32.as<float>(), lv.emask8.as<uint8_t>(), lv.wtab.as<float>(),
+                    lv.wdinv32.as<float>(),
                     l == 0 ? r32 : lv.vr.as<float>(), lv.vrp.as<float>(), M.levels[l + 1].vx.as<float>(),
                     l == 0 ? z : lv.vx.as<float>(), l == 0, (l == 0 && with_dot) ? &d : nullptr);
-        if (l == 0) c.mark(PK_UP0, true, (double)lv.n_node * (lv.wtab.p ? 3 * 16 + 1 : 3 * 20));
+        if (l == 0) c.mark(PK_UP0, true, (double)lv.n_node * 3 * 20);
     }
     c.mark(PK_VCYCLE, true);
 }
@@ -353,11 +341,8 @@ static int pcg_mixed(Model& M, const double* b, double* x, int32_t* iters_out, d
     }
     if (!std::isfinite(normB)) throw Error(GMGS_ERR_NONFINITE, "non-finite load vector");
     // algorithmic bytes per node: r64 rw, r32 read + write, q, p, wdinv, x rw
-    // (omega / diag comes from the element mask, already counted with the flags, when the level has the table)
-    const double jbytes = (double)l0.n_node * 3 * (16 + 8 + 4 + 4 + (l0.wtab.p ? 0 : 4) + 16) + 2.0 * (double)l0.n_node;
+    const double jbytes = (double)l0.n_node * 3 * (16 + 8 + 4 + 4 + 4 + 16) + 2.0 * (double)l0.n_node;
     const double pbytes = (double)l0.n_node * 3 * (4 + 4 + 4 + 4) + 2.0 * (double)l0.n_node;
-    const char* icvt_env = std::getenv("GMGS_INTCVT");
-    const int icvt = icvt_env ? std::atoi(icvt_env) : 0;
 
     // Fused kernel: the previous iteration's update (x += alpha p, r -= alpha q,
     // |r|^2 for its convergence test) followed by the next iteration's Jacobi
@@ -375,7 +360,6 @@ static int pcg_mixed(Model& M, const double* b, double* x, int32_t* iters_out, d
         a.scal = scal;
         a.cur = cur;
         a.first = first;
-        a.icvt = icvt;
         a.dot = dot_out(M, SC_RR);
         c.mark(PK_FINE_MATVEC, false);
         c.mark(PK_UPDATE_JACOBI, false);

@@ -30,6 +30,7 @@
 // Elements with their own stored matrix (coarse levels) and the nodes they
 // touch (NF_PEREL) are left to k_perel_vdown; the element rows of such
 // elements are zero here and PEREL nodes are not written.
+#include <cstdlib>
 #include <cstring>
 
 #include "fine.cuh"
@@ -49,9 +50,9 @@ constexpr int EOS = 36;                   // floats per element in the output bu
 constexpr int TC_COLS = 128;              // tensor-memory columns per CTA: A and D of two MMA groups
 constexpr int B_FLOATS = 32 * 24;
 constexpr int RING_FLOATS = (3 * 3 * SPL + 3) / 4 * 4;   // 2,676 floats: the next buffer stays 16-byte aligned
-constexpr size_t SMEM_BYTES = (size_t)(B_FLOATS + WTAB_FLOATS + RING_FLOATS + NTHR * EOS) * 4 + 16;   // + mbarrier, TMEM address, stop flag
-static_assert((B_FLOATS + WTAB_FLOATS + RING_FLOATS) % 4 == 0, "element-output buffer must be 16-byte aligned");
-static_assert((B_FLOATS + WTAB_FLOATS + RING_FLOATS + NTHR * EOS) % 2 == 0, "the mbarrier must be 8-byte aligned");
+constexpr size_t SMEM_BYTES = (size_t)(B_FLOATS + RING_FLOATS + NTHR * EOS) * 4 + 16;   // + mbarrier, TMEM address, stop flag
+static_assert((B_FLOATS + RING_FLOATS) % 4 == 0, "element-output buffer must be 16-byte aligned");
+static_assert((B_FLOATS + RING_FLOATS + NTHR * EOS) % 2 == 0, "the mbarrier must be 8-byte aligned");
 constexpr uint32_t IDESC = tc::idesc_tf32(128, 32);
 
 __device__ __forceinline__ int ring_slot(int z) { return (z + 3) % 3; }   // z >= -1
@@ -74,13 +75,25 @@ void make_tc_coef(const double* ke_rows, TcCoef& c) {
         }
 }
 
-__global__ void __launch_bounds__(NTHR, 4) k_tc_vdown(FineLevel L, const __grid_constant__ TcCoef cf,
+// Raw inputs of one staged point, loaded a layer before they are combined
+// into the field (so no thread waits on a load it has just issued).
+struct RawPoint {
+    float r[3], w[3];
+};
+// Raw data of this thread's element in one layer.
+struct RawElem {
+    uint32_t solid = 0;
+    int32_t type = 0;
+    float scale = 1.f;
+};
+
+template <int MINB>
+__global__ void __launch_bounds__(NTHR, MINB) k_tc_vdown(FineLevel L, const __grid_constant__ TcCoef cf,
                                                      const float* __restrict__ r32, const float* __restrict__ wdinv,
                                                      float* __restrict__ out, int zc, int* __restrict__ err) {
     extern __shared__ __align__(16) float smem[];
     float* Bs = smem;
-    float* stab = Bs + B_FLOATS;          // omega / diag by element mask (uniform level) or unused
-    float* ring = stab + WTAB_FLOATS;
+    float* ring = Bs + B_FLOATS;
     float* eout = ring + RING_FLOATS;
     uint64_t* mbar = reinterpret_cast<uint64_t*>(eout + NTHR * EOS);
     uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
@@ -104,9 +117,6 @@ __global__ void __launch_bounds__(NTHR, 4) k_tc_vdown(FineLevel L, const __grid_
     const int t = threadIdx.x, w = t >> 5, lane = t & 31;
 
     for (int i = t; i < B_FLOATS; i += NTHR) Bs[i] = cf.B[i];
-    const bool wt = L.wtab != nullptr;
-    if (wt)
-        for (int i = t; i < WTAB_FLOATS; i += NTHR) stab[i] = L.wtab[i];
     if (w == 0) {
         tc::tmem_alloc(tslot, TC_COLS);
         tc::tmem_relinquish();
@@ -134,31 +144,38 @@ __global__ void __launch_bounds__(NTHR, 4) k_tc_vdown(FineLevel L, const __grid_
     bool ok0, ok1 = false;
     const int base0 = point_slot(t, ok0);
     const int base1 = has_p1 ? point_slot(t + NTHR, ok1) : 0;
-    auto fetch = [&](int iz, float (&v0)[3], float (&v1)[3]) {
+    auto fetch = [&](int iz, RawPoint& p0, RawPoint& p1) {   // loads only
         const bool zok = iz >= 0 && iz <= g.nz;
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            v0[c] = 0.f;
-            v1[c] = 0.f;
-        }
         const long long n3 = 3ll * S;
         constexpr int F = chk::TC_FIELD;
-        auto point = [&](int i, float (&v)[3]) {
-            const int m3 = wt ? 3 * chk::ld(L.emask8, i, S, F) : 0;
 #pragma unroll
-            for (int c = 0; c < 3; ++c)
-                v[c] = chk::ld(r32, i + c * S, n3, F) * (wt ? stab[m3 + c] : chk::ld(wdinv, i + c * S, n3, F));
-        };
-        if (zok && ok0) point(base0 + iz * sz, v0);
-        if (zok && ok1) point(base1 + iz * sz, v1);
+        for (int c = 0; c < 3; ++c) {
+            p0.r[c] = p0.w[c] = p1.r[c] = p1.w[c] = 0.f;
+        }
+        if (zok && ok0) {
+            const int i = base0 + iz * sz;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                p0.r[c] = chk::ld(r32, i + c * S, n3, F);
+                p0.w[c] = chk::ld(wdinv, i + c * S, n3, F);
+            }
+        }
+        if (zok && ok1) {
+            const int i = base1 + iz * sz;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                p1.r[c] = chk::ld(r32, i + c * S, n3, F);
+                p1.w[c] = chk::ld(wdinv, i + c * S, n3, F);
+            }
+        }
     };
-    auto store = [&](int iz, const float (&v0)[3], const float (&v1)[3]) {
+    auto store = [&](int iz, const RawPoint& p0, const RawPoint& p1) {   // the field v = omega D^-1 r
         const int rs = ring_slot(iz) * 3 * SPL;
         constexpr long long R = 3 * 3 * SPL;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            chk::st(ring, rs + c * SPL + t, R, chk::TC_RING, v0[c]);
-            if (has_p1) chk::st(ring, rs + c * SPL + t + NTHR, R, chk::TC_RING, v1[c]);
+            chk::st(ring, rs + c * SPL + t, R, chk::TC_RING, p0.r[c] * p0.w[c]);
+            if (has_p1) chk::st(ring, rs + c * SPL + t + NTHR, R, chk::TC_RING, p1.r[c] * p1.w[c]);
         }
     };
 
@@ -166,13 +183,43 @@ __global__ void __launch_bounds__(NTHR, 4) k_tc_vdown(FineLevel L, const __grid_
     const int egy = ey0 + lane, egx = ex0 + w;
     const bool ecol = egy >= 0 && egx >= 0 && egy < g.ny && egx < g.nx;
     const int eslot0 = (egx + 1) * g.py + egy + Grid::YOFF + sz;
-    auto elem_scale = [&](int ez) -> float {   // 0 for void / foreign-matrix elements
-        if (!ecol || ez < 0 || ez >= g.nz) return 0.f;
+    auto elem_fetch = [&](int ez) {            // loads only
+        RawElem e;
+        if (!ecol || ez < 0 || ez >= g.nz) return e;
         const int es = eslot0 + ez * sz;
         constexpr int E = chk::TC_ELEM;
-        if (!chk::ld(L.emask, es, S, E)) return 0.f;
-        if (L.etype && chk::ld(L.etype, es, S, E) > 0) return 0.f;
-        return L.escale ? chk::ld(L.escale, es, S, E) : 1.f;
+        e.solid = chk::ld(L.emask, es, S, E);
+        if (L.etype) e.type = chk::ld(L.etype, es, S, E);
+        if (L.escale) e.scale = chk::ld(L.escale, es, S, E);
+        return e;
+    };
+    // the element's row scale: 0 for void elements and for those with their own matrix
+    auto elem_scale = [](const RawElem& e) { return (e.solid && e.type <= 0) ? e.scale : 0.f; };
+
+    // first differences of this thread's element in the layer whose node
+    // planes are in ring slots P0 (bottom) and P1 (top), times the row scale
+    auto gather = [&](int ez, float s, float (&a)[24]) {
+        const float* P0 = ring + ring_slot(ez) * 3 * SPL;
+        const float* P1 = ring + ring_slot(ez + 1) * 3 * SPL;
+        const int o = lane + w * SY;    // staged index of the element's origin node (dy = dx = 0)
+        constexpr long long R = 3 * SPL;
+        const float u[3] = {chk::ld(P0, o, R, chk::TC_RING), chk::ld(P0, SPL + o, R, chk::TC_RING),
+                            chk::ld(P0, 2 * SPL + o, R, chk::TC_RING)};
+#pragma unroll
+        for (int k = 0; k < 24; ++k) {
+            const int j = k / 3, b = k % 3;
+            const float* P = corner_z(j) ? P1 : P0;
+            a[k] = (chk::ld(P, b * SPL + o + corner_y(j) + corner_x(j) * SY, R, chk::TC_RING) - u[b]) * s;
+        }
+    };
+    auto store_a = [&](const float (&a)[24]) {
+#pragma unroll
+        for (int kk = 0; kk < 3; ++kk) {
+            float a8[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) a8[i] = a[8 * kk + i];
+            tc::tmem_st8(tb + lane_base + a_col + 8 * kk, a8);
+        }
     };
 
     // this thread's owned node (lane, w) for lane < 31, w < 7
@@ -182,48 +229,35 @@ __global__ void __launch_bounds__(NTHR, 4) k_tc_vdown(FineLevel L, const __grid_
     // element-output rows of the node's 4 elements in a layer: element (lane + 1 - dy, w + 1 - dx)
     const int erow00 = (lane + 1 + (w + 1) * EY) * EOS;
 
-    float v0[3], v1[3];
-    fetch(zb - 1, v0, v1);
-    store(zb - 1, v0, v1);
-    fetch(zb, v0, v1);
-    store(zb, v0, v1);
-    fetch(zb + 1, v0, v1);
-    float esc = elem_scale(zb - 1);
+    // prologue: node planes zb - 1 .. zb + 1 in the ring, plane zb + 2 loading,
+    // layer zb - 1 in the A operand, layer zb's element data loading
+    RawPoint p0, p1;
+    fetch(zb - 1, p0, p1);
+    store(zb - 1, p0, p1);
+    fetch(zb, p0, p1);
+    store(zb, p0, p1);
+    fetch(zb + 1, p0, p1);
+    store(zb + 1, p0, p1);
+    fetch(zb + 2, p0, p1);
+    RawElem en = elem_fetch(zb);
+    {
+        const float s = elem_scale(elem_fetch(zb - 1));
+        __syncthreads();
+        float a[24];
+        gather(zb - 1, s, a);
+        store_a(a);
+    }
     float part[3] = {0.f, 0.f, 0.f};         // top-corner sums of the previous layer for the current plane
     uint32_t nf = 0;                         // flags and residual of the plane the next layer finishes
     float rn[3] = {0.f, 0.f, 0.f};           // (loaded one layer ahead; plane zb - 1 is not owned)
-    __syncthreads();
 
     uint32_t phase = 0;
 #pragma unroll 1
     for (int ez = zb - 1; ez < ze; ++ez) {
-        // 1. this element's first differences -> A row in tensor memory
-        {
-            const float* P0 = ring + ring_slot(ez) * 3 * SPL;
-            const float* P1 = ring + ring_slot(ez + 1) * 3 * SPL;
-            const int o = lane + w * SY;    // staged index of the element's origin node (dy = dx = 0)
-            const float s = esc;
-            constexpr long long R = 3 * SPL;
-            const float u[3] = {chk::ld(P0, o, R, chk::TC_RING), chk::ld(P0, SPL + o, R, chk::TC_RING),
-                                chk::ld(P0, 2 * SPL + o, R, chk::TC_RING)};
-            // column k = 3 j + b of the A row: component b of local node j, in
-            // chunks of 8 columns (one tensor-memory store each)
-#pragma unroll
-            for (int kk = 0; kk < 3; ++kk) {
-                float a8[8];
-#pragma unroll
-                for (int i = 0; i < 8; ++i) {
-                    const int k = 8 * kk + i, j = k / 3, b = k % 3;
-                    const float* P = corner_z(j) ? P1 : P0;
-                    a8[i] = (chk::ld(P, b * SPL + o + corner_y(j) + corner_x(j) * SY, R, chk::TC_RING) - u[b]) * s;
-                }
-                tc::tmem_st8(tb + lane_base + a_col + 8 * kk, a8);
-            }
-        }
+        // A holds layer ez; the ring holds node planes ez .. ez + 2
         tc::tmem_wait_st();
         tc::fence_before_sync();
         __syncthreads();
-        // 2. one thread issues both MMA groups and commits them to the mbarrier
         if (t == 0) {
             tc::fence_after_sync();
             const uint32_t bsa = tc::smem_u32(Bs);
@@ -235,24 +269,24 @@ __global__ void __launch_bounds__(NTHR, 4) k_tc_vdown(FineLevel L, const __grid_
                                     IDESC, kk > 0);
             tc::mma_commit(mbar);
         }
-        // while the MMA runs: stage plane ez + 2 (its slot was last read by the
-        // previous layer's gather, before the barrier above), fetch plane ez + 3
-        // and the next layer's element data
-        store(ez + 2, v0, v1);
-        fetch(ez + 3, v0, v1);
-        const float esc_next = elem_scale(ez + 1);
-        // 3. wait for the MMA, read this element's outputs, publish them per corner
+        // while the MMA runs: the next layer's differences and element data
+        const bool more = ez + 1 < ze;
+        float a[24];
+        if (more) gather(ez + 1, elem_scale(en), a);
+        if (ez + 2 < ze) en = elem_fetch(ez + 2);
+        // wait for the MMA, then the next layer's rows replace this one's in A
         bool ok = tc::mbar_wait_bounded(mbar, phase);
         if (!ok) {
             atomicExch(err, 1);
             stop = 1;
             ok = tc::mbar_wait_bounded(mbar, phase);   // its writes must end before TMEM is freed
         }
-        ok = __all_sync(0xffffffffu, ok);               // tcgen05.ld is warp-collective
+        ok = __all_sync(0xffffffffu, ok);               // tcgen05.ld/st are warp-collective
         if (t == 0 && *reinterpret_cast<volatile int*>(err)) stop = 1;   // another CTA gave up
         phase ^= 1u;
         tc::fence_after_sync();
         if (ok) {
+            if (more) store_a(a);     // A is free once the MMA is done; storing first frees a's registers
             float d[3][8];
 #pragma unroll
             for (int kk = 0; kk < 3; ++kk) tc::tmem_ld8(tb + lane_base + d_col + 8 * kk, d[kk]);
@@ -271,7 +305,7 @@ __global__ void __launch_bounds__(NTHR, 4) k_tc_vdown(FineLevel L, const __grid_
         tc::fence_before_sync();
         __syncthreads();
         if (stop) break;
-        // 4. owned node: finish plane ez with this layer's bottom corners, start plane ez + 1
+        // owned node: finish plane ez with this layer's bottom corners, start plane ez + 1
         if (nown) {
             float yb[3] = {part[0], part[1], part[2]};
             float yt[3] = {0.f, 0.f, 0.f};
@@ -306,7 +340,12 @@ __global__ void __launch_bounds__(NTHR, 4) k_tc_vdown(FineLevel L, const __grid_
                 for (int c = 0; c < 3; ++c) rn[c] = chk::ld(r32, n + c * S, 3ll * S, chk::TC_NODE);
             }
         }
-        esc = esc_next;
+        // node plane ez + 3 into the ring slot of plane ez (no longer read),
+        // and the loads of plane ez + 4
+        if (ez + 2 < ze) {
+            store(ez + 3, p0, p1);
+            fetch(ez + 4, p0, p1);
+        }
     }
     tc::fence_before_sync();
     __syncthreads();
@@ -317,24 +356,32 @@ int tc_grid_blocks(const Grid& g, int zc) {
     return ((g.ny + 1 + NY - 1) / NY) * ((g.nx + 1 + NX - 1) / NX) * ((g.nz + 1 + zc - 1) / zc);
 }
 
-static int tc_zc(const Grid& g, const Ctx& c) {
+static int tc_zc(const Grid& g, const Ctx& c, int minb) {
     const int64_t cols = (int64_t)((g.ny + 1 + NY - 1) / NY) * ((g.nx + 1 + NX - 1) / NX);
-    const int64_t want = (int64_t)c.num_sms * 4 * 12;      // ~12 waves of 4 resident CTAs per SM
+    const int64_t want = (int64_t)c.num_sms * minb * 12;   // ~12 waves of the resident CTAs
     int64_t zc = (cols * (g.nz + 1) + want - 1) / want;
     return (int)std::min<int64_t>(64, std::max<int64_t>(8, zc));
 }
 
-void launch_tc_vdown(Ctx& c, const FineLevel& L, const TcCoef& cf, const float* r32, const float* wdinv, float* out,
-                     int* err) {
+template <int MINB>
+static void launch_tc_vdown_t(Ctx& c, const FineLevel& L, const TcCoef& cf, const float* r32, const float* wdinv,
+                              float* out, int* err) {
     static bool attr_set = false;    // per process; the attribute is a property of the function
     if (!attr_set) {
-        GMGS_CUDA(cudaFuncSetAttribute(k_tc_vdown, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
+        GMGS_CUDA(cudaFuncSetAttribute(k_tc_vdown<MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_BYTES));
         attr_set = true;
     }
-    const int zc = tc_zc(L.g, c);
+    const int zc = tc_zc(L.g, c, MINB);
     const dim3 grid((L.g.ny + 1 + NY - 1) / NY, (L.g.nx + 1 + NX - 1) / NX, (L.g.nz + 1 + zc - 1) / zc);
-    k_tc_vdown<<<grid, NTHR, SMEM_BYTES, c.stream>>>(L, cf, r32, wdinv, out, zc, err);
+    k_tc_vdown<MINB><<<grid, NTHR, SMEM_BYTES, c.stream>>>(L, cf, r32, wdinv, out, zc, err);
     GMGS_LAUNCHED(c);
+}
+
+void launch_tc_vdown(Ctx& c, const FineLevel& L, const TcCoef& cf, const float* r32, const float* wdinv, float* out,
+                     int* err) {
+    const char* e = std::getenv("GMGS_TC_MINB");
+    if (e && e[0] == '2') launch_tc_vdown_t<2>(c, L, cf, r32, wdinv, out, err);
+    else launch_tc_vdown_t<3>(c, L, cf, r32, wdinv, out, err);
 }
 
 // occupancy of the element-form kernel's 31 x 7 node tiles per z plane

@@ -87,22 +87,3 @@ def test_tc_mixed_solve_matches_oracle(name, monkeypatch):
     assert abs(s.iterations - o.iterations) <= 1
     assert rel(u, u_ref) < 1e-5
     s.close()
-
-
-@pytest.mark.parametrize("tc", ["0", "1"])
-def test_diagonal_table_is_bit_identical(tc, monkeypatch):
-    """On a uniform finest level the kernels take omega / diag from a table
-    indexed by the node's 8-element mask instead of the wdinv vector; the
-    table is summed like the diagonal kernel, so the mixed solve is bitwise
-    the same with and without it (GMGS_WTAB=0)."""
-    vox, fixed, loads, L, _ = _inputs("block42_L4")
-    monkeypatch.setenv("GMGS_TC", tc)
-    out = {}
-    for wt in ("1", "0"):
-        monkeypatch.setenv("GMGS_WTAB", wt)
-        s = Solver(vox, omega=0.4, num_levels=L, precision="mixed")
-        s.set_bc(fixed, loads)
-        out[wt] = (s.solve(), s.iterations)
-        s.close()
-    assert out["1"][1] == out["0"][1]
-    assert np.array_equal(out["1"][0], out["0"][0])

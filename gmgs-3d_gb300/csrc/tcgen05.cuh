@@ -119,6 +119,15 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* mbar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
+// one arrival of this thread on the mbarrier's current phase
+__device__ __forceinline__ void mbar_arrive(uint64_t* mbar) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(smem_u32(mbar))
+                 : "memory");
+}
+// barrier among `count` threads (a multiple of 32) of the CTA on named barrier `id` (1..15)
+__device__ __forceinline__ void named_sync(uint32_t id, uint32_t count) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
 __device__ __forceinline__ uint64_t globaltimer_ns() {
     uint64_t t;
     asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));

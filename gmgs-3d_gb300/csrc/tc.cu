@@ -110,9 +110,9 @@ __global__ void __launch_bounds__(NTHR, 2) k_tc_vdown(FineLevel L, const __grid_
     float* ring = Bs + B_FLOATS;
     float* eout = ring + RING_FLOATS;                                    // [2][NWORK * EOS]
     uint64_t* bars = reinterpret_cast<uint64_t*>(eout + 2 * EOUT_FLOATS);
-    uint64_t* a_full = bars;          // [2]: 256 worker arrivals
+    uint64_t* a_full = bars;          // [2]: one arrival per worker warp
     uint64_t* d_full = bars + 2;      // [2]: the MMA commit
-    uint64_t* d_empty = bars + 4;     // [2]: 256 worker arrivals after reading D
+    uint64_t* d_empty = bars + 4;     // [2]: one arrival per worker warp after reading D
     uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + NBAR);
     // flags[0]: the error flag was already set when this CTA started (read once, by thread 0);
     // flags[1 + (li & 1)]: a worker's wait in layer li ran out (written before that layer's worker
@@ -143,9 +143,9 @@ __global__ void __launch_bounds__(NTHR, 2) k_tc_vdown(FineLevel L, const __grid_
     }
     if (t == 0) {
         for (int s = 0; s < 2; ++s) {
-            tc::mbar_init(a_full + s, NWORK);
+            tc::mbar_init(a_full + s, NWORK / 32);    // one arrival per worker warp
             tc::mbar_init(d_full + s, 1);
-            tc::mbar_init(d_empty + s, NWORK);
+            tc::mbar_init(d_empty + s, NWORK / 32);
         }
         tc::mbar_fence_init();
         // an earlier CTA's tensor-core wait ran out: the result is void, skip the work
@@ -271,7 +271,8 @@ __global__ void __launch_bounds__(NTHR, 2) k_tc_vdown(FineLevel L, const __grid_
             }
             tc::tmem_wait_st();
             tc::fence_before_sync();
-            tc::mbar_arrive(a_full + s);
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(a_full + s);
         };
 
         // this thread's owned node (lane, w) for lane < 31, w < 7
@@ -329,7 +330,8 @@ __global__ void __launch_bounds__(NTHR, 2) k_tc_vdown(FineLevel L, const __grid_
                 for (int kk = 0; kk < 3; ++kk) tc::tmem_ld8(tb + lane_base + d_col(s, grp) + 8 * kk, d[kk]);
                 tc::tmem_wait_ld();
                 tc::fence_before_sync();
-                tc::mbar_arrive(d_empty + s);
+                __syncwarp();
+                if (lane == 0) tc::mbar_arrive(d_empty + s);
 #pragma unroll
                 for (int j = 0; j < 8; ++j) {
                     const int c = corner_y(j) + 2 * corner_x(j) + 4 * corner_z(j);

@@ -133,6 +133,19 @@ __device__ __forceinline__ uint64_t globaltimer_ns() {
     asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
     return t;
 }
+// try_wait that may suspend the thread for up to `hint_ns` until the phase
+// completes (a waiting warp then takes no issue slots)
+__device__ __forceinline__ bool mbar_try_wait_hint(uint64_t* mbar, uint32_t parity, uint32_t hint_ns) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(mbar)), "r"(parity), "r"(hint_ns)
+        : "memory");
+    return ok != 0;
+}
 // Bounded wait for the phase with the given parity to complete; false when
 // the time limit (default 20 ms; an MMA of these kernels takes microseconds)
 // runs out: the caller records an error and stops using the tensor cores.
@@ -140,7 +153,7 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* mbar, uint32_t parit
     if (mbar_try_wait(mbar, parity)) return true;
     const uint64_t t0 = globaltimer_ns();
     for (;;) {
-        if (mbar_try_wait(mbar, parity)) return true;
+        if (mbar_try_wait_hint(mbar, parity, 20000u)) return true;
         if (globaltimer_ns() - t0 > limit_ns) return false;
     }
 }

@@ -64,6 +64,7 @@ def parse():
     ap.add_argument("--omega", type=float, default=0.4)
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison solve")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-tc", action="store_true", help="skip the tensor-core down-sweep comparison")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle sample")
     ap.add_argument("--cpu-scale", type=float, default=0.25,
                     help="linear scale of the reduced model the CPU oracle is timed on")
@@ -406,6 +407,27 @@ def run_gmgs(a):
         ms = max_over_ranks(ms, "cuda")
 
     out = {}
+    if rank == 0 and not a.no_tc:
+        # the V-cycle down-sweep on the tensor cores (element form, tcgen05 kind::tf32;
+        # GMGS_TC=1) on the same handle, against the CUDA-core second-difference kernel
+        # timed above; the outer CG's kernels are the same in both
+        import numpy as np
+        u_cc = s.solve()
+        os.environ["GMGS_TC"] = "1"
+        try:
+            s.solve_dev(None)
+            ms_tc = timed(s, max(2, a.steps // 2))
+            n_tc, t_tc, _ = s.kernel_time(4)
+            u_tc = s.solve()
+            its_tc = s.iterations
+        finally:
+            os.environ.pop("GMGS_TC", None)
+        out["tensor_core_downsweep"] = {
+            "kernel": "k_tc_vdown (tcgen05 kind::tf32, warp-specialized, element form)",
+            "finest_downsweep_ms_per_launch": t_tc / max(n_tc, 1),
+            "cuda_core_downsweep_ms_per_launch": breakdown["fine_vcycle_down"]["ms_per_launch"],
+            "solve_s": ms_tc / 1e3, "iterations": its_tc,
+            "displacement_rel_diff_vs_cuda_core": float(np.linalg.norm(u_tc - u_cc) / np.linalg.norm(u_cc))}
     if rank == 0:
         # stress recovery on the solved state: nodal (f64) + per-voxel (6 f32)
         s.solve_dev(None)

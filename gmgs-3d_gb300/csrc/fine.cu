@@ -262,220 +262,6 @@ __global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? 3 : 5)
     if (MODE == FM_CG_DIRECTION || MODE == FM_CG_UPDATE_JACOBI) grid_dot_finish(dot.value(), a.dot, sh);
 }
 
-// ---------------------------------------------------------------------------
-// The CG update + Jacobi step (FM_CG_UPDATE_JACOBI) with its two halves in
-// different warps, so that the FP64 state update of one plane overlaps the
-// stencil of the next instead of following it behind the same barrier.
-// 16 warps per CTA on the 32 x 8 column tile of k_fine:
-//  * stencil warps (0-7): stage the field v = fl32(r32 - alpha q) * omega/diag
-//    of plane z + 1 in the four-plane ring, compute y = A v at the owned nodes
-//    of plane z (fixed rows zeroed) and hand y and v over through a
-//    double-buffered shared buffer;
-//  * update warps (8-15): one owned node each; the previous iteration's update
-//    and this iteration's Jacobi step in FP64 (x += alpha p + v, r -= alpha q
-//    + y, r32 = fl32(r), |r32 - alpha q|^2 for the convergence test), with
-//    their operands loaded one plane ahead.
-// Named barriers: 1 among the stencil warps (ring), 2 + b "plane in buffer b"
-// (stencil warps arrive, update warps wait), 4 + b "buffer b read" (update
-// warps arrive, stencil warps wait before refilling it).
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ void bar_arrive(uint32_t id, uint32_t count) {
-    asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(count) : "memory");
-}
-__device__ __forceinline__ void bar_sync(uint32_t id, uint32_t count) {
-    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
-}
-
-template <bool ICVT>
-__global__ void __launch_bounds__(2 * NT, 2)
-    k_cg_update_ws(FineLevel L, const __grid_constant__ Coef32 cf, FineArgs a, int zc) {
-    constexpr int MODE = FM_CG_UPDATE_JACOBI;
-    constexpr uint32_t ALL = 2 * NT;
-    __shared__ float ring[RING][3 * PLANE];
-    __shared__ float ybuf[2][6][NT];     // y (3) and v (3) of each tile node, node index lx * TY + ly
-    __shared__ double sh[32];
-    const Grid& g = L.g;
-    const int S = (int)g.slots;
-    const int sz = g.py * g.px;
-    const int y0 = blockIdx.x * TY, x0 = blockIdx.y * TX;
-    const int zb = blockIdx.z * zc;
-    const int ze = min(zb + zc, g.nz + 1);        // node planes [zb, ze)
-    if (L.tile_occ) {                             // no solid node in this column tile: nothing to compute
-        int any = 0;
-        for (int iz = zb; iz < ze; ++iz) any |= L.tile_occ[((int64_t)iz * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x];
-        if (!any) {
-            grid_dot_finish(0.0, a.dot, sh);
-            return;
-        }
-    }
-    const int nplanes = ze - zb;
-    const float alpha = a.first ? 0.f : (float)(a.scal[a.cur] / a.scal[2]);
-    Kahan dot;
-    if (threadIdx.x < NT) {
-        // ---------------------------------------------------------------- stencil warps
-        const int tid = threadIdx.x;
-        const int wrp = tid >> 5, lane = tid & 31;
-        const int ly = (wrp & 3) * 8 + (lane & 7), lx = (wrp >> 2) * 4 + (lane >> 3);
-        const int cy = y0 + ly, cx = x0 + lx;
-        const int pc = (ly + 1) + (lx + 1) * RP;
-        const bool ccol = cy <= g.ny + 1 && cx <= g.nx + 1;
-        const int cbase = (cx + 1) * g.py + (cy + Grid::YOFF) + sz;
-        int ph = 0, hbase = 0;
-        bool hcol = false;
-        if (tid < NHALO) {
-            int hy_, hx_;
-            if (tid < 2 * HX) { hy_ = (tid & 1) ? HY - 1 : 0; hx_ = tid >> 1; }
-            else { const int k = tid - 2 * HX; hx_ = (k & 1) ? HX - 1 : 0; hy_ = 1 + (k >> 1); }
-            ph = hy_ + hx_ * RP;
-            const int hy = y0 - 1 + hy_, hx = x0 - 1 + hx_;
-            hcol = hy >= -1 && hx >= -1 && hy <= g.ny + 1 && hx <= g.nx + 1;
-            hbase = (hx + 1) * g.py + (hy + Grid::YOFF) + sz;
-        }
-        auto fetch = [&](int iz, float vc[3], float vh[3]) {
-            vc[0] = vc[1] = vc[2] = 0.f;
-            vh[0] = vh[1] = vh[2] = 0.f;
-            const bool zok = iz >= -1 && iz <= g.nz + 1;
-            if (zok && ccol) field_at<MODE>(a, S, cbase + iz * sz, 0.f, alpha, vc);
-            if (zok && hcol) field_at<MODE>(a, S, hbase + iz * sz, 0.f, alpha, vh);
-        };
-        auto store = [&](float* r, const float vc[3], const float vh[3]) {
-            constexpr long long R = 3 * PLANE;
-#pragma unroll
-            for (int c = 0; c < 3; ++c) chk::st(r, pc + c * PLANE, R, chk::FINE_RING, vc[c]);
-            if (tid < NHALO) {
-#pragma unroll
-                for (int c = 0; c < 3; ++c) chk::st(r, ph + c * PLANE, R, chk::FINE_RING, vh[c]);
-            }
-        };
-        float vc[3], vh[3];
-        fetch(zb - 1, vc, vh);
-        store(ring[(zb - 1 + RING) % RING], vc, vh);
-        fetch(zb, vc, vh);
-        store(ring[zb % RING], vc, vh);
-        fetch(zb + 1, vc, vh);
-        const bool own = cy <= g.ny && cx <= g.nx;
-        uint32_t f_next = 0, e8_next = 0;
-        if (own) {
-            f_next = chk::ld(L.nflag, cbase + zb * sz, g.slots, chk::FINE_FLAGS);
-            e8_next = chk::ld(L.emask8, cbase + zb * sz, g.slots, chk::FINE_FLAGS);
-        }
-        const int node = lx * TY + ly;
-#pragma unroll 1
-        for (int k = 0; k < nplanes; ++k) {
-            const int iz = zb + k;
-            store(ring[(iz + 1) % RING], vc, vh);
-            bar_sync(1, NT);
-            if (iz + 2 <= g.nz + 1) fetch(iz + 2, vc, vh);
-            const uint32_t f = f_next, e8 = e8_next;
-            if (own && iz + 1 < ze) {
-                f_next = chk::ld(L.nflag, cbase + (iz + 1) * sz, g.slots, chk::FINE_FLAGS);
-                e8_next = chk::ld(L.emask8, cbase + (iz + 1) * sz, g.slots, chk::FINE_FLAGS);
-            }
-            const float* P0 = ring[(iz - 1 + RING) % RING];
-            const float* P1 = ring[iz % RING];
-            const float* P2 = ring[(iz + 1) % RING];
-            float y[3] = {0.f, 0.f, 0.f};
-            if (own && (f & NF_SOLID) && !(f & NF_PEREL)) {
-                const int n = cbase + iz * sz;
-                if (f & NF_INTERIOR) {
-                    interior_s<RP, PLANE>(cf, P0, P1, P2, pc, y[0], y[1], y[2]);
-                    y[0] *= L.kscale; y[1] *= L.kscale; y[2] *= L.kscale;
-                } else {
-                    boundary_s<RP, PLANE>(L, cf, e8, n, P0, P1, P2, pc, y[0], y[1], y[2]);
-                }
-                if (f & NF_FIX_X) y[0] = 0.f;
-                if (f & NF_FIX_Y) y[1] = 0.f;
-                if (f & NF_FIX_Z) y[2] = 0.f;
-            }
-            const int b = k & 1;
-            if (k >= 2) bar_sync(4 + b, ALL);              // the update warps have read buffer b
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                ybuf[b][c][node] = y[c];
-                ybuf[b][3 + c][node] = chk::ld(P1, pc + c * PLANE, 3 * PLANE, chk::FINE_RING);
-            }
-            bar_arrive(2 + b, ALL);                        // plane iz is in buffer b
-        }
-        // the update warps' "read" arrivals of the last two planes
-        for (int k = nplanes < 2 ? 0 : nplanes - 2; k < nplanes; ++k) bar_sync(4 + (k & 1), ALL);
-    } else {
-        // ---------------------------------------------------------------- update warps
-        const int e = threadIdx.x - NT;
-        const int ly = e & 31, lx = e >> 5;
-        const int cy = y0 + ly, cx = x0 + lx;
-        const bool own = cy <= g.ny && cx <= g.nx;
-        const int cbase = (cx + 1) * g.py + (cy + Grid::YOFF) + sz;
-        const int node = lx * TY + ly;
-        const long long n3 = 3ll * S;
-        constexpr int E = chk::FINE_EPI;
-        struct Ops {
-            uint32_t f;
-            float r[3], q[3], p[3];
-            double r64[3], x64[3];
-        };
-        auto load = [&](int iz, Ops& o) {
-            o.f = 0;
-            if (!own) return;
-            const int n = cbase + iz * sz;
-            o.f = chk::ld(L.nflag, n, S, E);
-            if (!(o.f & NF_SOLID) || (o.f & NF_PEREL)) return;
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                const int i = n + c * S;
-                o.r[c] = chk::ld(a.r32, i, n3, E);
-                o.r64[c] = chk::ld((const double*)a.r64, i, n3, E);
-                o.x64[c] = chk::ld((const double*)a.x64, i, n3, E);
-                if (!a.first) {
-                    o.q[c] = chk::ld(a.q32, i, n3, E);
-                    o.p[c] = chk::ld(a.pold, i, n3, E);
-                }
-            }
-        };
-        Ops cur, nxt;
-        load(zb, cur);
-#pragma unroll 1
-        for (int k = 0; k < nplanes; ++k) {
-            const int iz = zb + k;
-            if (k + 1 < nplanes) load(iz + 1, nxt);
-            const int b = k & 1;
-            bar_sync(2 + b, ALL);                          // plane iz is in buffer b
-            float y[3], v[3];
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                y[c] = ybuf[b][c][node];
-                v[c] = ybuf[b][3 + c][node];
-            }
-            bar_arrive(4 + b, ALL);                        // buffer b read
-            if (own && (cur.f & NF_SOLID) && !(cur.f & NF_PEREL)) {
-                const int n = cbase + iz * sz;
-                constexpr int O = chk::FINE_OUT;
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    // previous iteration's update x += alpha p, r -= alpha q (CG_solver.m:32-33),
-                    // then this iteration's Jacobi step x += dx, r -= A dx (CG_solver.m:18-19);
-                    // the caller removes the last dx when the solve stops
-                    const int i = n + c * S;
-                    float rinc = y[c], rm32 = cur.r[c], xinc = v[c];
-                    if (!a.first) {
-                        xinc = fmaf(alpha, cur.p[c], v[c]);
-                        rinc = fmaf(alpha, cur.q[c], rinc);
-                        rm32 = fmaf(-alpha, cur.q[c], rm32);
-                    }
-                    const double xd = ICVT ? f2d_int(xinc) : (double)xinc;
-                    const double rd = ICVT ? f2d_int(rinc) : (double)rinc;
-                    chk::st(a.x64, i, n3, O, cur.x64[c] + xd);
-                    const double rn = cur.r64[c] - rd;
-                    chk::st(a.r64, i, n3, O, rn);
-                    chk::st(a.r32out, i, n3, O, ICVT ? d2f_int(rn) : (float)rn);
-                    dot.add(rm32 * rm32);
-                }
-            }
-            cur = nxt;
-        }
-    }
-    grid_dot_finish(dot.value(), a.dot, sh);
-}
-
 static int pick_zc(const Grid& g, const Ctx& c) {
     const int64_t cols = (int64_t)((g.ny + 1 + TY - 1) / TY) * ((g.nx + 1 + TX - 1) / TX);
     // ~24 waves of 3 resident CTAs: shorter z-chunks balance the tail and let
@@ -504,14 +290,6 @@ template void launch_fine<FM_PLAIN>(Ctx&, const FineLevel&, const Coef32&, const
 template void launch_fine<FM_VCYCLE_DOWN>(Ctx&, const FineLevel&, const Coef32&, const FineArgs&);
 template void launch_fine<FM_CG_UPDATE_JACOBI>(Ctx&, const FineLevel&, const Coef32&, const FineArgs&);
 template void launch_fine<FM_CG_DIRECTION>(Ctx&, const FineLevel&, const Coef32&, const FineArgs&);
-
-void launch_cg_update_ws(Ctx& c, const FineLevel& L, const Coef32& cf, const FineArgs& a, bool icvt) {
-    const int zc = pick_zc(L.g, c);
-    dim3 grid((L.g.ny + 1 + TY - 1) / TY, (L.g.nx + 1 + TX - 1) / TX, (L.g.nz + 1 + zc - 1) / zc);
-    if (icvt) k_cg_update_ws<true><<<grid, 2 * NT, 0, c.stream>>>(L, cf, a, zc);
-    else k_cg_update_ws<false><<<grid, 2 * NT, 0, c.stream>>>(L, cf, a, zc);
-    GMGS_LAUNCHED(c);
-}
 
 // ---------------------------------------------------------------------------
 // V-cycle up-sweep in FP32 with omega D^-1 precomputed (Vcycle.m:29-32):

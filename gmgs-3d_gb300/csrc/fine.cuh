@@ -70,38 +70,6 @@ __host__ __device__ constexpr bool s_nonzero(int k, int a, int b) {
 }
 
 // ---------------------------------------------------------------------------
-// FP32 <-> FP64 conversions on the integer pipe.  GB300 runs conversions
-// between float and double on its FP64 pipe, at the rate of DADD (about 2
-// lanes per clock per SM, measured); the CG update needs three per DOF.
-// Both functions equal the hardware conversion bit for bit (checked on the
-// host over all 2^32 floats and 2^28 doubles with planted ties).
-// ---------------------------------------------------------------------------
-// float -> double: the exponent is re-biased and the 23 mantissa bits move to
-// the top of the 52.  Zero, subnormal, infinite and NaN inputs take the
-// hardware conversion.
-__device__ __forceinline__ double f2d_int(float f) {
-    const uint32_t u = __float_as_uint(f);
-    const uint32_t e = (u >> 23) & 0xFFu;
-    if (e == 0u || e == 0xFFu) return (double)f;
-    const uint32_t hi = (u & 0x80000000u) | (((u & 0x7FFFFFFFu) >> 3) + 0x38000000u);
-    return __hiloint2double((int)hi, (int)(u << 29));
-}
-// double -> float, round to nearest even: the 23 leading mantissa bits, plus
-// one when the dropped 29 bits are above half an ulp, or exactly half with an
-// odd result (a carry out of the mantissa raises the exponent, as it should).
-// Results outside the normal float range, zero, infinities and NaN take the
-// hardware conversion.
-__device__ __forceinline__ float d2f_int(double d) {
-    const uint32_t hi = (uint32_t)__double2hiint(d), lo = (uint32_t)__double2loint(d);
-    const uint32_t e = (hi >> 20) & 0x7FFu;
-    if (e < 897u || e > 1150u) return (float)d;
-    uint32_t t = ((e - 896u) << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29);
-    const uint32_t half = (lo >> 28) & 1u, rest = (lo & 0x0FFFFFFFu) != 0u;
-    t += half & (rest | (t & 1u));
-    return __uint_as_float((hi & 0x80000000u) | t);
-}
-
-// ---------------------------------------------------------------------------
 // reductions
 // ---------------------------------------------------------------------------
 struct Kahan {
@@ -286,9 +254,6 @@ int up32_grid_blocks(const Grid& gf);
 
 template <int MODE>
 void launch_fine(Ctx& c, const FineLevel& L, const Coef32& cf, const FineArgs& a);
-// FM_CG_UPDATE_JACOBI with the stencil and the FP64 update in separate warps
-// (icvt: FP32<->FP64 conversions on the integer pipe)
-void launch_cg_update_ws(Ctx& c, const FineLevel& L, const Coef32& cf, const FineArgs& a, bool icvt);
 
 void launch_up32(Ctx& c, const Grid& gf, const Grid& gc, const uint8_t* nflag, const uint8_t* tile_occ,
                  const float* wdinv, const float* r, const float* rp, const float* xc, float* xf, bool zero_fixed,

@@ -343,10 +343,6 @@ static int pcg_mixed(Model& M, const double* b, double* x, int32_t* iters_out, d
     // algorithmic bytes per node: r64 rw, r32 read + write, q, p, wdinv, x rw
     const double jbytes = (double)l0.n_node * 3 * (16 + 8 + 4 + 4 + 4 + 16) + 2.0 * (double)l0.n_node;
     const double pbytes = (double)l0.n_node * 3 * (4 + 4 + 4 + 4) + 2.0 * (double)l0.n_node;
-    // CG update kernel (environment GMGS_UJ): 0 one warp role, 1 stencil and
-    // FP64 update in separate warps, 2 the same with the conversions on the integer pipe
-    const char* uj_env = std::getenv("GMGS_UJ");
-    const int uj_mode = uj_env ? std::atoi(uj_env) : 0;
 
     // Fused kernel: the previous iteration's update (x += alpha p, r -= alpha q,
     // |r|^2 for its convergence test) followed by the next iteration's Jacobi
@@ -367,8 +363,7 @@ static int pcg_mixed(Model& M, const double* b, double* x, int32_t* iters_out, d
         a.dot = dot_out(M, SC_RR);
         c.mark(PK_FINE_MATVEC, false);
         c.mark(PK_UPDATE_JACOBI, false);
-        if (uj_mode == 0) launch_l0<FM_CG_UPDATE_JACOBI>(M, f0, a);
-        else launch_cg_update_ws(c, f0, M.coef, a, uj_mode == 2);
+        launch_l0<FM_CG_UPDATE_JACOBI>(M, f0, a);
         c.mark(PK_FINE_MATVEC, true, jbytes);
         c.mark(PK_UPDATE_JACOBI, true, jbytes);
         std::swap(r32a, r32b);

@@ -216,21 +216,3 @@ def test_solve_into_caller_buffer():
     with pytest.raises(ValueError):
         s.solve(out=np.zeros(u.size + 3))
 
-
-@pytest.mark.parametrize("mode", ["1", "2"])
-def test_cg_update_kernels_agree_bitwise(mode, monkeypatch):
-    """The CG update + Jacobi step with the stencil and the FP64 update in
-    separate warps (GMGS_UJ=1; =2 with the exact integer-pipe conversions)
-    does per node the arithmetic of the single-role kernel, so the mixed
-    solve gives bitwise the same displacement in the same iterations."""
-    vox = synthetic.make("block42_fp64")[0]
-    fixed, loads = synthetic.boundary_conditions(vox, 4)
-    out = {}
-    for m in ("0", mode):
-        monkeypatch.setenv("GMGS_UJ", m)
-        s = Solver(vox, omega=0.4, num_levels=4, precision="mixed")
-        s.set_bc(fixed, loads)
-        out[m] = (s.solve(), s.iterations)
-        s.close()
-    assert out[mode][1] == out["0"][1]
-    assert np.array_equal(out[mode][0], out["0"][0])

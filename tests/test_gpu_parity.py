@@ -216,3 +216,28 @@ def test_solve_into_caller_buffer():
     with pytest.raises(ValueError):
         s.solve(out=np.zeros(u.size + 3))
 
+
+
+@pytest.mark.parametrize("density", [False, True])
+def test_mixed_stress_matches_oracle_on_same_displacement(density):
+    """The mixed path recovers stress in FP32 arithmetic on a double-float
+    split of U (hi + lo); on the same displacement the oracle's FP64 maps
+    (GetCartesianStress.m:11-41 and the per-voxel centre stress) agree to
+    FP32 accuracy."""
+    vox = synthetic.sphere_voids(28, 24, 32, 2, 5)
+    fixed, loads = synthetic.boundary_conditions(vox, 3)
+    rho = synthetic.density(int(vox.sum()), (0.3, 1.0), 5) if density else None
+    s = Solver(vox, omega=0.4, num_levels=3, precision="mixed")
+    s.set_bc(fixed, loads)
+    o = Oracle(vox, Params(omega=0.4, num_levels=3))
+    o.apply_boundary_condition(fixed, loads)
+    if density:
+        s.set_density(rho, 3.0)
+        o.set_density(rho, 3.0)
+    u = s.solve()
+    o.setup()
+    o.U = u
+    nodal_ref, vox_ref = o.get_cartesian_stress()
+    nodal, vox6 = s.stress()
+    assert rel(nodal, nodal_ref) < 2e-6
+    assert rel(vox6, vox_ref) < 2e-6

@@ -45,6 +45,15 @@ int guarded(gmgs_handle* h, F&& f) {
         return st;
     } catch (const gmgs::Error& e) {
         g_last_error = e.what();
+#ifdef GMGS_CHECKED
+        // an out-of-range access is the likelier cause of a failure in a checked build
+        std::string m;
+        if (gmgs::chk::report(m)) {
+            g_last_error = m + " (the call then failed: " + e.what() + ")";
+            if (h) h->M.err = g_last_error;
+            return GMGS_ERR_CUDA;
+        }
+#endif
         if (h) h->M.err = e.what();
         return e.status;
     } catch (const std::bad_alloc&) {

@@ -224,7 +224,7 @@ __global__ void __launch_bounds__(NTHR, 2) k_tc_vdown(FineLevel L, const __grid_
         };
         auto store = [&](int iz, const RawPoint& p0, const RawPoint& p1) {   // the field v = omega D^-1 r
             const int rs = ring_slot(iz) * 3 * SPL;
-            constexpr long long R = 3 * 3 * SPL;
+            constexpr long long R = RING * 3 * SPL;
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
                 chk::st(ring, rs + c * SPL + t, R, chk::TC_RING, p0.r[c] * p0.w[c]);

@@ -21,11 +21,15 @@
 // (the reference's AtX states 0/1/2, src/kernel/AtX.m:1-58).
 // Fixed DOF rows are zeroed (AtX.m:57).
 //
-// FP64 is used only where the outer CG keeps its state: x and r are FP64
-// vectors updated with FP32-formed increments; dot products sum FP32 products
-// with per-thread compensated (Kahan) FP32 sums and FP64 across threads and
-// blocks.  (GB300 issues FP64 arithmetic at 2 operations per clock per SM,
-// 1/64 of its FP32 rate, and the FP32<->FP64 conversions use the same pipe.)
+// The outer CG keeps x and r as double-float vectors (hi + lo, two FP32
+// arrays, about 48 significant bits) updated with FP32-formed increments by
+// two-sums on the FP32 pipe; the high part of r is the FP32 residual the
+// stencil reads.  Dot products sum FP32 products with per-thread compensated
+// (Kahan) FP32 sums and FP64 across threads and blocks.  (GB300 issues FP64
+// arithmetic and FP32<->FP64 conversions at about 2 lanes per clock per SM,
+// 1/64 of its FP32 rate: in FP64 the five operations per DOF of the state
+// update kept that pipe 53 % busy and the kernel at 2.41 ms on the 153M-DOF
+// model.)
 #include "fine.cuh"
 
 namespace gmgs {
@@ -65,36 +69,14 @@ void make_stencil(const double* ke_rows, Coef32& cf) {
 // ---------------------------------------------------------------------------
 // the fused streaming kernel
 // ---------------------------------------------------------------------------
-// input field at one point (3 components) from the kernel's inputs
-template <int MODE>
-__device__ __forceinline__ void field_at(const FineArgs& a, int S, int s, float beta, float alpha, float v[3]) {
-    const long long n3 = 3ll * S;
-    constexpr int F = chk::FINE_FIELD;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        const int i = s + c * S;
-        if (MODE == FM_PLAIN) {
-            v[c] = chk::ld(a.v, i, n3, F);
-        } else if (MODE == FM_VCYCLE_DOWN) {
-            v[c] = chk::ld(a.r32, i, n3, F) * chk::ld(a.wdinv, i, n3, F);
-        } else if (MODE == FM_CG_UPDATE_JACOBI) {
-            const float r = chk::ld(a.r32, i, n3, F);
-            const float rm = a.first ? r : fmaf(-alpha, chk::ld(a.q32, i, n3, F), r);
-            v[c] = rm * chk::ld(a.wdinv, i, n3, F);
-        } else {   // FM_CG_DIRECTION
-            const float z = chk::ld(a.z32, i, n3, F);
-            v[c] = a.first ? z : fmaf(beta, chk::ld(a.pold, i, n3, F), z);
-        }
-    }
-}
-
 // per-node epilogue inputs, loaded before the stencil arithmetic of the plane
 struct EpiData {
     float r[3];       // FM_VCYCLE_DOWN: r;  FM_CG_UPDATE_JACOBI: r32
     float q[3];       // FM_CG_UPDATE_JACOBI
     float pp[3];      // FM_CG_UPDATE_JACOBI: p
-    double r64[3];    // FM_CG_UPDATE_JACOBI
-    double x64[3];    // FM_CG_UPDATE_JACOBI: loaded with the other operands, before the stencil
+    float rl[3];      // FM_CG_UPDATE_JACOBI: low part of r
+    float xh[3];      // FM_CG_UPDATE_JACOBI: x, loaded with the other operands, before the stencil
+    float xl[3];
 };
 
 template <int MODE>
@@ -107,8 +89,9 @@ __device__ __forceinline__ void epi_fetch(const FineArgs& a, int S, int n, EpiDa
         if (MODE == FM_VCYCLE_DOWN) d.r[c] = chk::ld(a.r32, i, n3, E);
         if (MODE == FM_CG_UPDATE_JACOBI) {
             d.r[c] = chk::ld(a.r32, i, n3, E);
-            d.r64[c] = chk::ld((const double*)a.r64, i, n3, E);
-            d.x64[c] = chk::ld((const double*)a.x64, i, n3, E);
+            d.rl[c] = chk::ld((const float*)a.r_lo, i, n3, E);
+            d.xh[c] = chk::ld((const float*)a.x_hi, i, n3, E);
+            d.xl[c] = chk::ld((const float*)a.x_lo, i, n3, E);
             if (!a.first) {
                 d.q[c] = chk::ld(a.q32, i, n3, E);
                 d.pp[c] = chk::ld(a.pold, i, n3, E);
@@ -118,7 +101,7 @@ __device__ __forceinline__ void epi_fetch(const FineArgs& a, int S, int n, EpiDa
 }
 
 // 48 registers (5 CTAs per SM) for the stencil-only modes; the CG update
-// holds FP64 state and keeps 80 registers (3 CTAs) without spilling.
+// holds the state update's operands and keeps 80 registers (3 CTAs).
 // Measured on the 153M-DOF model: 5 CTAs/SM took the down-sweep from 1.16 to
 // 1.13 ms and the direction kernel from 1.26 to 1.22 ms against 4 CTAs/SM.
 template <int MODE>
@@ -246,10 +229,13 @@ __global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? 3 : 5)
                         rinc = fmaf(alpha, ed.q[b], rinc);
                         rm32 = fmaf(-alpha, ed.q[b], rm32);
                     }
-                    chk::st(a.x64, i, n3, O, ed.x64[b] + (double)xinc);
-                    const double rn = ed.r64[b] - (double)rinc;
-                    chk::st(a.r64, i, n3, O, rn);
-                    chk::st(a.r32out, i, n3, O, (float)rn);
+                    float xh = ed.xh[b], xl = ed.xl[b], rh = ed.r[b], rl = ed.rl[b];
+                    df_add(xh, xl, xinc);
+                    df_add(rh, rl, -rinc);
+                    chk::st(a.x_hi, i, n3, O, xh);
+                    chk::st(a.x_lo, i, n3, O, xl);
+                    chk::st(a.r_lo, i, n3, O, rl);
+                    chk::st(a.r32out, i, n3, O, rh);
                     dot.add(rm32 * rm32);
                 } else {
                     chk::st(a.pout, i, n3, O, v);
@@ -426,21 +412,42 @@ int up32_grid_blocks(const Grid& g) {
     return ((g.ny + 1 + TY - 1) / TY) * ((g.nx + 1 + TX - 1) / TX) * ((g.nz + 1 + 1) / 2);
 }
 
-// x -= the last, not yet cancelled Jacobi step dx = fl32(fl32(r32 - alpha q) * w)
-__global__ void k_drop_last_dx(int64_t n, double* __restrict__ x, const float* __restrict__ r32,
-                               const float* __restrict__ q, const float* __restrict__ w,
-                               const double* __restrict__ scal, int cur, int first) {
+// (x_hi, x_lo) -= the last, not yet cancelled Jacobi step dx = fl32(fl32(r32 - alpha q) * w),
+// then x = x_hi + x_lo in FP64 (exact: the parts' 48 bits fit a double)
+__global__ void k_drop_last_dx(int64_t n, double* __restrict__ x, float* __restrict__ xh, float* __restrict__ xl,
+                               const float* __restrict__ r32, const float* __restrict__ q,
+                               const float* __restrict__ w, const double* __restrict__ scal, int cur, int first) {
     const float alpha = first ? 0.f : (float)(scal[cur] / scal[2]);
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const float rm = first ? r32[i] : fmaf(-alpha, q[i], r32[i]);
         const float dx = rm * w[i];
-        if (dx != 0.f) x[i] -= (double)dx;
+        float h = xh[i], l = xl[i];
+        if (dx != 0.f) {
+            df_add(h, l, -dx);
+            xh[i] = h;
+            xl[i] = l;
+        }
+        x[i] = f2d_int(h) + f2d_int(l);
     }
 }
-void launch_drop_last_dx(Ctx& c, int64_t n, double* x, const float* r32, const float* q, const float* w,
-                         const double* scal, int cur, int first) {
+void launch_drop_last_dx(Ctx& c, int64_t n, double* x, float* x_hi, float* x_lo, const float* r32, const float* q,
+                         const float* w, const double* scal, int cur, int first) {
     const int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)c.num_sms * 16);
-    k_drop_last_dx<<<blocks, 256, 0, c.stream>>>(n, x, r32, q, w, scal, cur, first);
+    k_drop_last_dx<<<blocks, 256, 0, c.stream>>>(n, x, x_hi, x_lo, r32, q, w, scal, cur, first);
+    GMGS_LAUNCHED(c);
+}
+
+__global__ void k_df_split(int64_t n, const double* __restrict__ b, float* __restrict__ hi, float* __restrict__ lo) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double v = b[i];
+        const float h = d2f_int(v);
+        hi[i] = h;
+        lo[i] = d2f_int(v - f2d_int(h));
+    }
+}
+void launch_df_split(Ctx& c, int64_t n, const double* b, float* hi, float* lo) {
+    const int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)c.num_sms * 16);
+    k_df_split<<<blocks, 256, 0, c.stream>>>(n, b, hi, lo);
     GMGS_LAUNCHED(c);
 }
 

@@ -37,14 +37,14 @@ enum FineMode {
     FM_VCYCLE_DOWN = 1,       // v = w r, out = r - A v               (Vcycle.m:14, JacobiSmoother.m:5-9)
     FM_CG_UPDATE_JACOBI = 2,  // previous CG update r_m = r - alpha q, x += alpha p, r_m.r_m;
                               // then the Jacobi step v = fl32(w r_m), x += v, r = r_m - A v
-                              //                                  (CG_solver.m:31-35, 18-19)
+                              // (x and r double-float)           (CG_solver.m:31-35, 18-19)
     FM_CG_DIRECTION = 3       // v = fl32(z + beta p_old), p = v, q = A v, p.q  (CG_solver.m:23-31)
 };
 
 struct FineArgs {
     const float* v = nullptr;        // FM_PLAIN input
-    const float* r32 = nullptr;      // FM_VCYCLE_DOWN / FM_CG_UPDATE_JACOBI residual in FP32 (read on the halo)
-    double* r64 = nullptr;           // FM_CG_UPDATE_JACOBI residual in FP64 (owned nodes, updated in place)
+    const float* r32 = nullptr;      // FM_VCYCLE_DOWN residual; FM_CG_UPDATE_JACOBI: its high part (read on the halo)
+    float* r_lo = nullptr;           // FM_CG_UPDATE_JACOBI residual, low part (owned nodes, updated in place)
     const float* wdinv = nullptr;    // omega / diag (3 planes)
     const float* z32 = nullptr;      // FM_CG_DIRECTION preconditioned residual
     const float* pold = nullptr;     // previous direction (FM_CG_DIRECTION: p_{k-1}; FM_CG_UPDATE_JACOBI: p_k)
@@ -53,8 +53,9 @@ struct FineArgs {
     int cur = 0, first = 0;
     float* out32 = nullptr;          // y / r' / q
     float* pout = nullptr;           // new direction (must not alias pold)
-    double* x64 = nullptr;           // solution (owned nodes, in place)
-    float* r32out = nullptr;         // FP32 copy of the updated residual (must not alias r32)
+    float* x_hi = nullptr;           // solution, double-float high and low parts (owned nodes, in place)
+    float* x_lo = nullptr;
+    float* r32out = nullptr;         // high part of the updated residual (must not alias r32)
     DotOut dot;
 };
 
@@ -122,6 +123,29 @@ __device__ inline void grid_dot_finish(double v, const DotOut& d, double* sh) {
         if (tid == 0) {
             *d.out = t;
             *d.ticket = 0;
+        }
+    }
+}
+
+// input field at one point (3 components) from the kernel's inputs
+template <int MODE>
+__device__ __forceinline__ void field_at(const FineArgs& a, int S, int s, float beta, float alpha, float v[3]) {
+    const long long n3 = 3ll * S;
+    constexpr int F = chk::FINE_FIELD;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const int i = s + c * S;
+        if (MODE == FM_PLAIN) {
+            v[c] = chk::ld(a.v, i, n3, F);
+        } else if (MODE == FM_VCYCLE_DOWN) {
+            v[c] = chk::ld(a.r32, i, n3, F) * chk::ld(a.wdinv, i, n3, F);
+        } else if (MODE == FM_CG_UPDATE_JACOBI) {
+            const float r = chk::ld(a.r32, i, n3, F);
+            const float rm = a.first ? r : fmaf(-alpha, chk::ld(a.q32, i, n3, F), r);
+            v[c] = rm * chk::ld(a.wdinv, i, n3, F);
+        } else {   // FM_CG_DIRECTION
+            const float z = chk::ld(a.z32, i, n3, F);
+            v[c] = a.first ? z : fmaf(beta, chk::ld(a.pold, i, n3, F), z);
         }
     }
 }
@@ -254,6 +278,9 @@ int up32_grid_blocks(const Grid& gf);
 
 template <int MODE>
 void launch_fine(Ctx& c, const FineLevel& L, const Coef32& cf, const FineArgs& a);
+// the same modes (but FM_CG_UPDATE_JACOBI) four nodes per thread, f32x2 arithmetic (quad.cu); bit-identical outputs
+template <int MODE>
+void launch_fine4(Ctx& c, const FineLevel& L, const Coef32& cf, const FineArgs& a);
 
 void launch_up32(Ctx& c, const Grid& gf, const Grid& gc, const uint8_t* nflag, const uint8_t* tile_occ,
                  const float* wdinv, const float* r, const float* rp, const float* xc, float* xf, bool zero_fixed,
@@ -265,7 +292,10 @@ void launch_emask8(Ctx& c, const Grid& g, const uint8_t* emask, uint8_t* e8);
 size_t tile_occ_bytes(const Grid& g);
 void launch_tile_occ(Ctx& c, const Grid& g, const uint8_t* nflag, uint8_t* occ);
 void launch_to_f32(Ctx& c, int64_t n, const double* a, float* b);
-void launch_drop_last_dx(Ctx& c, int64_t n, double* x, const float* r32, const float* q, const float* w,
-                         const double* scal, int cur, int first);
+// x = x_hi + x_lo - (the last Jacobi step), written in FP64
+void launch_drop_last_dx(Ctx& c, int64_t n, double* x, float* x_hi, float* x_lo, const float* r32, const float* q,
+                         const float* w, const double* scal, int cur, int first);
+// b -> (hi, lo) = (fl32(b), fl32(b - hi))
+void launch_df_split(Ctx& c, int64_t n, const double* b, float* hi, float* lo);
 
 }  // namespace gmgs

@@ -92,6 +92,31 @@ template <typename T, typename I, typename V>
 __device__ __forceinline__ void st(T* p, I i, long long n, int site, V v) {
     if (ok((long long)i, n, site)) p[i] = (T)v;
 }
+// W-wide vector access at element i: i must be a multiple of W and i + W <= n
+template <int W>
+__device__ __forceinline__ bool okv(long long i, long long n, int site) {
+    return ok(i, i % W == 0 ? n - (W - 1) : 0, site);
+}
+template <typename I>
+__device__ __forceinline__ float4 ld4(const float* p, I i, long long n, int site) {
+    return okv<4>((long long)i, n, site) ? *reinterpret_cast<const float4*>(p + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+}
+template <typename I>
+__device__ __forceinline__ void st4(float* p, I i, long long n, int site, float4 v) {
+    if (okv<4>((long long)i, n, site)) *reinterpret_cast<float4*>(p + i) = v;
+}
+template <typename I>
+__device__ __forceinline__ float2 ld2(const float* p, I i, long long n, int site) {
+    return okv<2>((long long)i, n, site) ? *reinterpret_cast<const float2*>(p + i) : make_float2(0.f, 0.f);
+}
+template <typename I>
+__device__ __forceinline__ void st2(float* p, I i, long long n, int site, float2 v) {
+    if (okv<2>((long long)i, n, site)) *reinterpret_cast<float2*>(p + i) = v;
+}
+template <typename I>
+__device__ __forceinline__ uint32_t ld_u8x4(const uint8_t* p, I i, long long n, int site) {
+    return okv<4>((long long)i, n, site) ? *reinterpret_cast<const uint32_t*>(p + i) : 0u;
+}
 // host: each translation unit registers a reader of its own device words
 using Reader = bool (*)(std::string& msg);
 void add_reader(Reader r);
@@ -124,8 +149,63 @@ template <typename T, typename I>
 __device__ __forceinline__ T ld(const T* p, I i, long long, int) { return p[i]; }
 template <typename T, typename I, typename V>
 __device__ __forceinline__ void st(T* p, I i, long long, int, V v) { p[i] = (T)v; }
+template <typename I>
+__device__ __forceinline__ float4 ld4(const float* p, I i, long long, int) {
+    return *reinterpret_cast<const float4*>(p + i);
+}
+template <typename I>
+__device__ __forceinline__ void st4(float* p, I i, long long, int, float4 v) { *reinterpret_cast<float4*>(p + i) = v; }
+template <typename I>
+__device__ __forceinline__ float2 ld2(const float* p, I i, long long, int) {
+    return *reinterpret_cast<const float2*>(p + i);
+}
+template <typename I>
+__device__ __forceinline__ void st2(float* p, I i, long long, int, float2 v) { *reinterpret_cast<float2*>(p + i) = v; }
+template <typename I>
+__device__ __forceinline__ uint32_t ld_u8x4(const uint8_t* p, I i, long long, int) {
+    return *reinterpret_cast<const uint32_t*>(p + i);
+}
 #endif
 }  // namespace chk
+
+// ---------------------------------------------------------------------------
+// FP32 <-> FP64 without the FP64 pipe, and double-float sums
+// ---------------------------------------------------------------------------
+// GB300 runs FP64 adds and FP32<->FP64 conversions at about 2 lanes per clock
+// per SM, 1/64 of its FP32 rate.  float -> double and double -> float (round
+// to nearest even) with integer operations, equal to the hardware conversions
+// bit for bit; values outside the normal float range, zero, infinities and NaN
+// take the hardware path.
+__device__ __forceinline__ double f2d_int(float f) {
+    const uint32_t u = __float_as_uint(f);
+    const uint32_t e = (u >> 23) & 0xFFu;
+    if (e == 0u || e == 0xFFu) return (double)f;
+    const uint32_t hi = (u & 0x80000000u) | (((u & 0x7FFFFFFFu) >> 3) + 0x38000000u);
+    return __hiloint2double((int)hi, (int)(u << 29));
+}
+__device__ __forceinline__ float d2f_int(double d) {
+    const uint32_t hi = (uint32_t)__double2hiint(d), lo = (uint32_t)__double2loint(d);
+    const uint32_t e = (hi >> 20) & 0x7FFu;
+    if (e < 897u || e > 1150u) return (float)d;
+    uint32_t t = ((e - 896u) << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+    const uint32_t half = (lo >> 28) & 1u, rest = (lo & 0x0FFFFFFFu) != 0u;
+    t += half & (rest | (t & 1u));
+    return __uint_as_float((hi & 0x80000000u) | t);
+}
+
+// (hi, lo) += a for a double-float hi + lo (|lo| <= ulp(hi) / 2): Knuth's
+// branch-free two-sum of hi + a (exact: s + e = hi + a), the low parts added,
+// then Dekker's fast two-sum renormalises.  The sum keeps about 48 significant
+// bits (relative error ~2^-47 per update), all on the FP32 pipe.
+__device__ __forceinline__ void df_add(float& hi, float& lo, float a) {
+    const float s = __fadd_rn(hi, a);
+    const float bv = __fsub_rn(s, hi);
+    const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bv)), __fsub_rn(a, bv));
+    const float t = __fadd_rn(e, lo);
+    const float h = __fadd_rn(s, t);
+    lo = __fsub_rn(t, __fsub_rn(h, s));
+    hi = h;
+}
 
 // ---------------------------------------------------------------------------
 // grid geometry

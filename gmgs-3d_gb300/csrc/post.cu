@@ -124,26 +124,6 @@ __global__ void __launch_bounds__(128) k_stress_voxel(Grid g, StressCoef cf, con
 // is formed as (hi_j - hi_0) + (lo_j - lo_0): relative error about 2^-24 of
 // the difference itself, so the stresses keep FP32 relative accuracy.
 // ---------------------------------------------------------------------------
-// float -> double and double -> float (round to nearest even) with integer
-// operations, equal to the hardware conversions bit for bit; values outside
-// the normal float range, zero, infinities and NaN take the hardware path
-__device__ __forceinline__ double f2d_int(float f) {
-    const uint32_t u = __float_as_uint(f);
-    const uint32_t e = (u >> 23) & 0xFFu;
-    if (e == 0u || e == 0xFFu) return (double)f;
-    const uint32_t hi = (u & 0x80000000u) | (((u & 0x7FFFFFFFu) >> 3) + 0x38000000u);
-    return __hiloint2double((int)hi, (int)(u << 29));
-}
-__device__ __forceinline__ float d2f_int(double d) {
-    const uint32_t hi = (uint32_t)__double2hiint(d), lo = (uint32_t)__double2loint(d);
-    const uint32_t e = (hi >> 20) & 0x7FFu;
-    if (e < 897u || e > 1150u) return (float)d;
-    uint32_t t = ((e - 896u) << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29);
-    const uint32_t half = (lo >> 28) & 1u, rest = (lo & 0x0FFFFFFFu) != 0u;
-    t += half & (rest | (t & 1u));
-    return __uint_as_float((hi & 0x80000000u) | t);
-}
-
 __global__ void k_split_hilo(int64_t n, const double* __restrict__ U, float* __restrict__ hi, float* __restrict__ lo) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const double u = chk::ld(U, i, n, chk::STRESS_U);

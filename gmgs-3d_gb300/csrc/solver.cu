@@ -97,6 +97,12 @@ static bool tc_enabled() {
     return e && e[0] == '1';
 }
 
+// the stencil-only modes four nodes per thread (quad.cu) when GMGS_QUAD=1
+static bool quad_enabled() {
+    const char* e = std::getenv("GMGS_QUAD");
+    return e && (e[0] == '1' || e[0] == '3');
+}
+
 // A tensor-core kernel whose wait on its MMA ran out sets the device flag;
 // the solve reports it instead of returning a result computed without it.
 static void check_tc(Model& M) {
@@ -151,6 +157,7 @@ void vcycle_apply(Model& M, const double* r, double* z) {
     const int64_t n3 = 3 * M.levels[0].g.slots;
     if (M.prm.precision == GMGS_MIXED) {
         M.use_tc = tc_enabled();
+        M.use_quad = quad_enabled();
         launch_copy<float, double>(M.ctx, n3, M.cg_r32.as<float>(), r);
         vcycle32(M, M.cg_r32.as<float>(), M.cg_z32.as<float>(), false, 0);
         launch_copy<double, float>(M.ctx, n3, z, M.cg_z32.as<float>());
@@ -188,6 +195,12 @@ static FineLevel fine_level(const Level& lv) {
 
 template <int MODE>
 static void launch_l0(Model& M, const FineLevel& f, const FineArgs& a) {
+    if constexpr (MODE != FM_CG_UPDATE_JACOBI) {
+        if (M.use_quad) {
+            launch_fine4<MODE>(M.ctx, f, M.coef, a);
+            return;
+        }
+    }
     launch_fine<MODE>(M.ctx, f, M.coef, a);
 }
 
@@ -226,7 +239,8 @@ static void vcycle32(Model& M, const float* r32, float* z, bool with_dot, int do
         } else if (l == 0) {
             launch_l0<FM_VCYCLE_DOWN>(M, fl, a);
         } else if (lv.n_perel < lv.n_node) {
-            launch_fine<FM_VCYCLE_DOWN>(c, fl, M.coef, a);
+            if (M.use_quad) launch_fine4<FM_VCYCLE_DOWN>(c, fl, M.coef, a);
+            else launch_fine<FM_VCYCLE_DOWN>(c, fl, M.coef, a);
         }
         if (lv.n_perel > 0)
             launch_perel_vdown(c, fl, M.coef, lv.perel_nodes.as<int32_t>(), (int)lv.n_perel, a.r32, a.wdinv,
@@ -313,11 +327,16 @@ static bool capture_iteration_graphs(Model& M, Body& body) {
 static int pcg_mixed(Model& M, const double* b, double* x, int32_t* iters_out, double* relres_out, double* hist) {
     Ctx& c = M.ctx;
     M.use_tc = tc_enabled();
+    M.use_quad = quad_enabled();
     Level& l0 = M.levels[0];
     const int64_t n3 = 3 * l0.g.slots;
     double* scal = M.scal.as<double>();
     const DotScratch ds = dots(M);
-    double* r64 = M.cg_r.as<double>();
+    // double-float state: x = x_hi + x_lo in the two halves of cg_x, r = r32 + r_lo
+    // (the high part double-buffered, the low part in the first half of cg_r)
+    float* x_hi = M.cg_x.as<float>();
+    float* x_lo = x_hi + n3;
+    float* r_lo = M.cg_r.as<float>();
     float* r32a = M.cg_r32.as<float>();
     float* r32b = M.cg_r32b.as<float>();
     float* pa = M.cg_pa.as<float>();
@@ -327,12 +346,13 @@ static int pcg_mixed(Model& M, const double* b, double* x, int32_t* iters_out, d
 
     launch_dot<double, double>(c, ds, n3, b, b, scal + SC_BB);
     GMGS_CUDA(cudaMemcpyAsync(M.scal_host + SC_BB, scal + SC_BB, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
-    GMGS_CUDA(cudaMemsetAsync(x, 0, n3 * sizeof(double), c.stream));
-    GMGS_CUDA(cudaMemcpyAsync(r64, b, n3 * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));   // r = b - A*0
-    launch_to_f32(c, n3, b, r32a);
+    GMGS_CUDA(cudaMemsetAsync(x_hi, 0, 2 * n3 * sizeof(float), c.stream));
+    launch_df_split(c, n3, b, r32a, r_lo);     // r = b - A*0
     GMGS_CUDA(cudaStreamSynchronize(c.stream));
     const double normB = std::sqrt(M.scal_host[SC_BB]);
     if (normB == 0.0) {
+        GMGS_CUDA(cudaMemsetAsync(x, 0, n3 * sizeof(double), c.stream));
+        GMGS_CUDA(cudaStreamSynchronize(c.stream));
         if (iters_out) *iters_out = 0;
         if (relres_out) *relres_out = 0;
         M.last_iters = 0;
@@ -340,8 +360,8 @@ static int pcg_mixed(Model& M, const double* b, double* x, int32_t* iters_out, d
         return GMGS_OK;
     }
     if (!std::isfinite(normB)) throw Error(GMGS_ERR_NONFINITE, "non-finite load vector");
-    // algorithmic bytes per node: r64 rw, r32 read + write, q, p, wdinv, x rw
-    const double jbytes = (double)l0.n_node * 3 * (16 + 8 + 4 + 4 + 4 + 16) + 2.0 * (double)l0.n_node;
+    // algorithmic bytes per node: r (high part read + write, low part rw), q, p, wdinv, x (both parts rw)
+    const double jbytes = (double)l0.n_node * 3 * (8 + 8 + 4 + 4 + 4 + 16) + 2.0 * (double)l0.n_node;
     const double pbytes = (double)l0.n_node * 3 * (4 + 4 + 4 + 4) + 2.0 * (double)l0.n_node;
 
     // Fused kernel: the previous iteration's update (x += alpha p, r -= alpha q,
@@ -351,11 +371,12 @@ static int pcg_mixed(Model& M, const double* b, double* x, int32_t* iters_out, d
     auto update_jacobi = [&](int first, int cur) {
         FineArgs a;
         a.r32 = r32a;
-        a.r64 = r64;
+        a.r_lo = r_lo;
         a.q32 = q;
         a.pold = pa;
         a.wdinv = l0.wdinv32.as<float>();
-        a.x64 = x;
+        a.x_hi = x_hi;
+        a.x_lo = x_lo;
         a.r32out = r32b;
         a.scal = scal;
         a.cur = cur;
@@ -458,7 +479,7 @@ static int pcg_mixed(Model& M, const double* b, double* x, int32_t* iters_out, d
     }
     // the last fused launch already applied the Jacobi step of an iteration
     // that does not run; its inputs (r32 it read, q, alpha) are still in place
-    launch_drop_last_dx(c, n3, x, r32b, q, l0.wdinv32.as<float>(), scal, its & 1, 0);
+    launch_drop_last_dx(c, n3, x, x_hi, x_lo, r32b, q, l0.wdinv32.as<float>(), scal, its & 1, 0);
     GMGS_CUDA(cudaStreamSynchronize(c.stream));
     check_tc(M);
     if (status == GMGS_ERR_MAX_ITERATIONS && M.prm.verbose) std::printf("Exceed the maximum iterate numbers\n");

@@ -53,7 +53,7 @@ enum gmgs_status {
 
 enum gmgs_precision {
     GMGS_FP64 = 0,   /* plain FP64 V-cycle PCG: the drop-in for the reference solve */
-    GMGS_MIXED = 1   /* FP32 V-cycle, FP64 outer CG vectors, dots and coarsest solve */
+    GMGS_MIXED = 1   /* FP32 V-cycle, double-float (2 x FP32) outer CG state, FP64 dots, coarsest solve and U */
 };
 
 /* Solver controls; the reference's globals (src/GlobalVariables.m:3-23). */

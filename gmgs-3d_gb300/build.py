@@ -25,8 +25,7 @@ CSRC = PKG / "csrc"
 BUILD = ROOT / "_build" / "gmgs"
 LIB = PKG / "gmgs" / "libgmgs.so"
 LIB_CHECKED = PKG / "gmgs" / "libgmgs_checked.so"
-SOURCES = ["api.cu", "setup.cu", "operators.cu", "solver.cu", "post.cu", "fine.cu", "quad.cu", "tc.cu", "noalloc.cu",
-           "voxelize.cu",
+SOURCES = ["api.cu", "setup.cu", "operators.cu", "solver.cu", "post.cu", "fine.cu", "tc.cu", "noalloc.cu", "voxelize.cu",
            "coarse.cu"]
 # the voxeliser decides inside/outside by exact FP64 comparisons: no FMA contraction
 FILE_FLAGS = {"voxelize.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]}

@@ -278,9 +278,6 @@ int up32_grid_blocks(const Grid& gf);
 
 template <int MODE>
 void launch_fine(Ctx& c, const FineLevel& L, const Coef32& cf, const FineArgs& a);
-// the same modes (but FM_CG_UPDATE_JACOBI) four nodes per thread, f32x2 arithmetic (quad.cu); bit-identical outputs
-template <int MODE>
-void launch_fine4(Ctx& c, const FineLevel& L, const Coef32& cf, const FineArgs& a);
 
 void launch_up32(Ctx& c, const Grid& gf, const Grid& gc, const uint8_t* nflag, const uint8_t* tile_occ,
                  const float* wdinv, const float* r, const float* rp, const float* xc, float* xf, bool zero_fixed,

@@ -92,31 +92,6 @@ template <typename T, typename I, typename V>
 __device__ __forceinline__ void st(T* p, I i, long long n, int site, V v) {
     if (ok((long long)i, n, site)) p[i] = (T)v;
 }
-// W-wide vector access at element i: i must be a multiple of W and i + W <= n
-template <int W>
-__device__ __forceinline__ bool okv(long long i, long long n, int site) {
-    return ok(i, i % W == 0 ? n - (W - 1) : 0, site);
-}
-template <typename I>
-__device__ __forceinline__ float4 ld4(const float* p, I i, long long n, int site) {
-    return okv<4>((long long)i, n, site) ? *reinterpret_cast<const float4*>(p + i) : make_float4(0.f, 0.f, 0.f, 0.f);
-}
-template <typename I>
-__device__ __forceinline__ void st4(float* p, I i, long long n, int site, float4 v) {
-    if (okv<4>((long long)i, n, site)) *reinterpret_cast<float4*>(p + i) = v;
-}
-template <typename I>
-__device__ __forceinline__ float2 ld2(const float* p, I i, long long n, int site) {
-    return okv<2>((long long)i, n, site) ? *reinterpret_cast<const float2*>(p + i) : make_float2(0.f, 0.f);
-}
-template <typename I>
-__device__ __forceinline__ void st2(float* p, I i, long long n, int site, float2 v) {
-    if (okv<2>((long long)i, n, site)) *reinterpret_cast<float2*>(p + i) = v;
-}
-template <typename I>
-__device__ __forceinline__ uint32_t ld_u8x4(const uint8_t* p, I i, long long n, int site) {
-    return okv<4>((long long)i, n, site) ? *reinterpret_cast<const uint32_t*>(p + i) : 0u;
-}
 // host: each translation unit registers a reader of its own device words
 using Reader = bool (*)(std::string& msg);
 void add_reader(Reader r);
@@ -149,22 +124,6 @@ template <typename T, typename I>
 __device__ __forceinline__ T ld(const T* p, I i, long long, int) { return p[i]; }
 template <typename T, typename I, typename V>
 __device__ __forceinline__ void st(T* p, I i, long long, int, V v) { p[i] = (T)v; }
-template <typename I>
-__device__ __forceinline__ float4 ld4(const float* p, I i, long long, int) {
-    return *reinterpret_cast<const float4*>(p + i);
-}
-template <typename I>
-__device__ __forceinline__ void st4(float* p, I i, long long, int, float4 v) { *reinterpret_cast<float4*>(p + i) = v; }
-template <typename I>
-__device__ __forceinline__ float2 ld2(const float* p, I i, long long, int) {
-    return *reinterpret_cast<const float2*>(p + i);
-}
-template <typename I>
-__device__ __forceinline__ void st2(float* p, I i, long long, int, float2 v) { *reinterpret_cast<float2*>(p + i) = v; }
-template <typename I>
-__device__ __forceinline__ uint32_t ld_u8x4(const uint8_t* p, I i, long long, int) {
-    return *reinterpret_cast<const uint32_t*>(p + i);
-}
 #endif
 }  // namespace chk
 

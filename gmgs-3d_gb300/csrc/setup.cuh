@@ -40,7 +40,6 @@ struct Model {
     TcCoef tcoef{};                                            // Ke as the tensor cores' B operand
     DevBuf tc_err;         // int: set when a tensor-core wait ran out
     bool use_tc = false;   // V-cycle down-sweeps on the tensor cores (environment GMGS_TC)
-    bool use_quad = false; // stencil-only fine kernels four nodes per thread (environment GMGS_QUAD)
     DevBuf scal;           // device scalars (see solver.cu)
     DevBuf dot_partials, dot_ticket;
     // CUDA graphs of the mixed PCG iteration body (one per parity), valid for

@@ -97,12 +97,6 @@ static bool tc_enabled() {
     return e && e[0] == '1';
 }
 
-// the stencil-only modes four nodes per thread (quad.cu) when GMGS_QUAD=1
-static bool quad_enabled() {
-    const char* e = std::getenv("GMGS_QUAD");
-    return e && (e[0] == '1' || e[0] == '3');
-}
-
 // A tensor-core kernel whose wait on its MMA ran out sets the device flag;
 // the solve reports it instead of returning a result computed without it.
 static void check_tc(Model& M) {
@@ -157,7 +151,6 @@ void vcycle_apply(Model& M, const double* r, double* z) {
     const int64_t n3 = 3 * M.levels[0].g.slots;
     if (M.prm.precision == GMGS_MIXED) {
         M.use_tc = tc_enabled();
-        M.use_quad = quad_enabled();
         launch_copy<float, double>(M.ctx, n3, M.cg_r32.as<float>(), r);
         vcycle32(M, M.cg_r32.as<float>(), M.cg_z32.as<float>(), false, 0);
         launch_copy<double, float>(M.ctx, n3, z, M.cg_z32.as<float>());
@@ -195,12 +188,6 @@ static FineLevel fine_level(const Level& lv) {
 
 template <int MODE>
 static void launch_l0(Model& M, const FineLevel& f, const FineArgs& a) {
-    if constexpr (MODE != FM_CG_UPDATE_JACOBI) {
-        if (M.use_quad) {
-            launch_fine4<MODE>(M.ctx, f, M.coef, a);
-            return;
-        }
-    }
     launch_fine<MODE>(M.ctx, f, M.coef, a);
 }
 
@@ -239,8 +226,7 @@ static void vcycle32(Model& M, const float* r32, float* z, bool with_dot, int do
         } else if (l == 0) {
             launch_l0<FM_VCYCLE_DOWN>(M, fl, a);
         } else if (lv.n_perel < lv.n_node) {
-            if (M.use_quad) launch_fine4<FM_VCYCLE_DOWN>(c, fl, M.coef, a);
-            else launch_fine<FM_VCYCLE_DOWN>(c, fl, M.coef, a);
+            launch_fine<FM_VCYCLE_DOWN>(c, fl, M.coef, a);
         }
         if (lv.n_perel > 0)
             launch_perel_vdown(c, fl, M.coef, lv.perel_nodes.as<int32_t>(), (int)lv.n_perel, a.r32, a.wdinv,
@@ -327,7 +313,6 @@ static bool capture_iteration_graphs(Model& M, Body& body) {
 static int pcg_mixed(Model& M, const double* b, double* x, int32_t* iters_out, double* relres_out, double* hist) {
     Ctx& c = M.ctx;
     M.use_tc = tc_enabled();
-    M.use_quad = quad_enabled();
     Level& l0 = M.levels[0];
     const int64_t n3 = 3 * l0.g.slots;
     double* scal = M.scal.as<double>();

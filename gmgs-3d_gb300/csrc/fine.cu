@@ -129,9 +129,16 @@ __global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? 3 : 5)
     const int wrp = tid >> 5, lane = tid & 31;
     const int ly = (wrp & 3) * 8 + (lane & 7), lx = (wrp >> 2) * 4 + (lane >> 3);
 
+    // beta = r.z / r_old.z_old, alpha = r.z / p.q: one FP64 division per CTA
+    // instead of one per thread on GB300's narrow FP64 pipe
     float beta = 0.f, alpha = 0.f;
-    if (MODE == FM_CG_DIRECTION && !a.first) beta = (float)(a.scal[a.cur] / a.scal[a.cur ^ 1]);
-    if (MODE == FM_CG_UPDATE_JACOBI && !a.first) alpha = (float)(a.scal[a.cur] / a.scal[2]);
+    if ((MODE == FM_CG_DIRECTION || MODE == FM_CG_UPDATE_JACOBI) && !a.first) {
+        __shared__ float s_ab;
+        if (threadIdx.x == 0 && threadIdx.y == 0)
+            s_ab = (float)(a.scal[a.cur] / a.scal[MODE == FM_CG_DIRECTION ? (a.cur ^ 1) : 2]);
+        __syncthreads();
+        (MODE == FM_CG_DIRECTION ? beta : alpha) = s_ab;
+    }
 
     // this thread's centre point and (for tid < NHALO) one halo point of every plane
     const int cy = y0 + ly, cx = x0 + lx;
@@ -437,12 +444,18 @@ void launch_drop_last_dx(Ctx& c, int64_t n, double* x, float* x_hi, float* x_lo,
     GMGS_LAUNCHED(c);
 }
 
+// (the load vector is zero almost everywhere: zeros, tested on the integer
+// pipe, skip the FP64 subtraction)
 __global__ void k_df_split(int64_t n, const double* __restrict__ b, float* __restrict__ hi, float* __restrict__ lo) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const double v = b[i];
-        const float h = d2f_int(v);
+        float h = 0.f, l = 0.f;
+        if ((__double_as_longlong(v) << 1) != 0) {
+            h = d2f_int(v);
+            l = d2f_int(v - f2d_int(h));
+        }
         hi[i] = h;
-        lo[i] = d2f_int(v - f2d_int(h));
+        lo[i] = l;
     }
 }
 void launch_df_split(Ctx& c, int64_t n, const double* b, float* hi, float* lo) {

@@ -391,6 +391,7 @@ void factor_coarse(Ctx& c, CoarseBlocks& cb, const std::function<void()>& overla
             gemm(h, {Op::T, Op::N, 0, false}, B, B, B, 1.0, Eb(k + 1), B, Db(k + 1), B, 0.0, t2[1].as<double>(), B);
     }
     if (overlap) overlap();
+    c.trace_point("bc: work buffers (beside the factorisation)");
     for (int h = 0; h < 2; ++h) {
         GMGS_CUDA(cudaEventRecord(ev[1 + h], st[h]));
         GMGS_CUDA(cudaStreamWaitEvent(c.stream, ev[1 + h], 0));

@@ -492,6 +492,48 @@ __global__ void k_diag(Grid g, const uint8_t* __restrict__ emask, const uint8_t*
     }
 }
 
+// On a level whose solid elements all carry kscale * Ke0 (no per-element
+// matrices, no element scales) a node's diagonal depends only on which of its
+// 8 elements are solid: the 256 masks' sums (in k_diag's element order, each
+// product and sum rounded separately), then one table lookup per node.
+__device__ __forceinline__ void diag_of_mask(uint32_t mask, const double* __restrict__ ke0, double kscale,
+                                             const double* __restrict__ escale, double a[3]) {
+    a[0] = a[1] = a[2] = 0.0;
+    for (int e = 0; e < 8; ++e) {
+        if (!((mask >> e) & 1u)) continue;
+        const int A = e & 1, B = (e >> 1) & 1, C = e >> 2;
+        const int c = corner_of(A, B, C);
+        for (int al = 0; al < 3; ++al) {
+            const int ii = (3 * c + al) * 24 + 3 * c + al;
+            a[al] = __dadd_rn(a[al], __dmul_rn(__dmul_rn(kscale, escale ? escale[0] : 1.0), ke0[ii]));
+        }
+    }
+}
+__global__ void k_diag_table(const double* __restrict__ ke0, double kscale, const double* __restrict__ escale,
+                             double* __restrict__ table) {
+    const uint32_t m = threadIdx.x;   // one thread per mask, 256 threads
+    double a[3];
+    diag_of_mask(m, ke0, kscale, escale, a);
+    for (int al = 0; al < 3; ++al) table[3 * m + al] = a[al];
+}
+__global__ void k_diag_uniform(Grid g, const uint8_t* __restrict__ emask, const uint8_t* __restrict__ nflag,
+                               const double* __restrict__ table, double* __restrict__ d) {
+    __shared__ double t[3 * 256];
+    for (int i = threadIdx.x; i < 3 * 256; i += blockDim.x) t[i] = table[i];
+    __syncthreads();
+    GRID_STRIDE(s, g.slots) {
+        uint32_t mask = 0;
+        if (nflag[s] & NF_SOLID)
+            for (int e = 0; e < 8; ++e) {
+                const int A = e & 1, B = (e >> 1) & 1, C = e >> 2;
+                if (emask[s - A - B * g.sx() - C * g.sz()]) mask |= 1u << e;
+            }
+        d[s] = t[3 * mask];
+        d[s + g.slots] = t[3 * mask + 1];
+        d[s + 2 * g.slots] = t[3 * mask + 2];
+    }
+}
+
 // Level-2 diagonal when its element matrices are the scaled-children sums
 // sum_j s_j G_j and only their FP32 copies are kept: each element's diagonal
 // entry is summed exactly as k_galerkin sums it, so the result equals k_diag
@@ -952,6 +994,14 @@ void build_operators(Model& M) {
                 k_diag_children<<<blocks_for(c, lv.g.slots), 256, 0, c.stream>>>(
                     lv.g, l0.g, lv.emask.as<uint8_t>(), lv.nflag.as<uint8_t>(), l0.emask.as<uint8_t>(),
                     l0.escale64.as<double>(), l0.kscale, M.galerkin_child.as<double>(), lv.diag64.as<double>());
+            } else if (!lv.etype.p && !(l == 0 && lv.escale64.p)) {
+                DevBuf table = dalloc(3 * 256 * sizeof(double));
+                k_diag_table<<<1, 256, 0, c.stream>>>(ke0, lv.kscale, nullptr, table.as<double>());
+                GMGS_LAUNCHED(c);
+                k_diag_uniform<<<blocks_for(c, lv.g.slots), 256, 0, c.stream>>>(
+                    lv.g, lv.emask.as<uint8_t>(), lv.nflag.as<uint8_t>(), table.as<double>(), lv.diag64.as<double>());
+                GMGS_LAUNCHED(c);
+                GMGS_CUDA(cudaStreamSynchronize(c.stream));
             } else {
                 k_diag<<<blocks_for(c, lv.g.slots), 256, 0, c.stream>>>(
                     lv.g, lv.emask.as<uint8_t>(), lv.nflag.as<uint8_t>(), lv.etype.as<int32_t>(), lv.Ks64.as<double>(),

@@ -143,11 +143,15 @@ __global__ void __launch_bounds__(256) k_chol_inv32(double* __restrict__ A, int 
         if (t > j && t < 32) a[j][t] *= dinv;                  // L(t, j)
         if (t >= 32 && t - 32 <= j) x[t - 32][j] *= dinv;      // X(j, c), c <= j
         __syncthreads();
-        for (int e = t; e < 1024; e += 256) {
-            const int cc = e >> 5, r = e & 31;
-            if (r > j) {
-                if (cc > j && r >= cc) a[cc][r] = fma(-a[j][r], a[j][cc], a[cc][r]);
-                if (cc <= j) x[cc][r] = fma(-a[j][r], x[cc][j], x[cc][r]);
+        // only rows r > j change: (31 - j) rows x 32 columns, column cc of row r
+        // of A (j < cc <= r) or of X (cc <= j); the same update per element as a
+        // full sweep, in the same column order
+        for (int e = t; e < 32 * (31 - j); e += 256) {
+            const int r = j + 1 + (e >> 5), cc = e & 31;
+            if (cc > j) {
+                if (r >= cc) a[cc][r] = fma(-a[j][r], a[j][cc], a[cc][r]);
+            } else {
+                x[cc][r] = fma(-a[j][r], x[cc][j], x[cc][r]);
             }
         }
         __syncthreads();

@@ -550,7 +550,7 @@ def run_gmgs(a):
     line = {
         "metric": METRIC, "value": ms / 1e3, "unit": "s", "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 V-cycle / double-f32 CG state", "data": "synthetic",
+        "dtype": "f32 V-cycle; x, r double-f32; dots f32 products, f64 sums; f64 coarsest solve", "data": "synthetic",
         "config": {"workload": a.workload, "resolution": [w.nelx, w.nely, w.nelz], "voids": w.voids,
                    "levels": L, "padded": list(s.padded_dims), "dofs": dofs, "omega": a.omega, "tol": w.tol,
                    "iterations": its, "relres": relres, "l2": "inputs larger than L2 (no flush)",
@@ -634,7 +634,7 @@ def run_mesh(a):
         "metric": METRIC + " (reference demo mesh)", "value": mx["solve_s"], "unit": "s", "n_gpus": 1,
         "steps": a.steps, "warmup": a.warmup, "ms_per_step": mx["solve_s"] * 1e3, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": (mx["solve_s"] / a.published_s) if a.published_s else None,
-        "dtype": "f32 V-cycle / double-f32 CG state", "data": f"mesh {Path(a.mesh).name} with its demo boundary conditions",
+        "dtype": "f32 V-cycle; x, r double-f32; dots f32 products, f64 sums; f64 coarsest solve", "data": f"mesh {Path(a.mesh).name} with its demo boundary conditions",
         "config": {"workload": f"{Path(a.mesh).stem}_{a.res}", "grid_ny_nx_nz": mx["grid"], "dofs": mx["dofs"],
                    "levels": mx["levels"], "omega": 0.4, "tol": 1e-3, "iterations": mx["iterations"],
                    "relres": mx["relres"], "published_s": a.published_s},

@@ -41,6 +41,7 @@ def nvcc() -> str:
 
 def flags(debug: bool) -> list[str]:
     f = ["-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", str(ROOT / "include"), "-I", str(CSRC),
+         "-I", str(BUILD),
          "--expt-relaxed-constexpr", "-Xptxas", "-v" if os.environ.get("GMGS_PTXAS_V") else "-O3"]
     f += ["-O0", "-g", "-DGMGS_CHECKED"] if debug else ["-O3"]
     return ARCH + f
@@ -52,10 +53,37 @@ def obj_dir(debug: bool) -> Path:
     return BUILD / ("debug" if debug else "release")
 
 
+# the default-material coefficient table the streaming kernels include
+# (generated from the library's host element code by gen_default_stencil.cu)
+DEFAULT_STENCIL = BUILD / "gmgs_default_stencil.h"
+
+
+def generate_default_stencil() -> Path:
+    gen_src = CSRC / "gen_default_stencil.cu"
+    deps = [gen_src, CSRC / "element_host.h", CSRC / "gmgs_internal.cuh"]
+    exe = BUILD / "gen_default_stencil"
+    # regenerated on every machine that builds (the generator's executable is
+    # not carried between machines): the host arithmetic may differ by platform
+    if (DEFAULT_STENCIL.exists() and exe.exists()
+            and all(DEFAULT_STENCIL.stat().st_mtime >= d.stat().st_mtime for d in deps)):
+        return DEFAULT_STENCIL
+    BUILD.mkdir(parents=True, exist_ok=True)
+    cmd = [nvcc(), "-std=c++17", "-O3", "-I", str(ROOT / "include"), "-I", str(CSRC), str(gen_src), "-o", str(exe)]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"nvcc failed for gen_default_stencil.cu:\n{res.stdout}\n{res.stderr}")
+    tmp = DEFAULT_STENCIL.with_suffix(".tmp")
+    res = subprocess.run([str(exe), str(tmp)], capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"gen_default_stencil failed:\n{res.stdout}\n{res.stderr}")
+    tmp.replace(DEFAULT_STENCIL)
+    return DEFAULT_STENCIL
+
+
 def compile_one(src: str, debug: bool) -> Path:
     out = obj_dir(debug) / (Path(src).stem + ".o")
     srcp = CSRC / src
-    deps = [srcp] + list(CSRC.glob("*.cuh")) + [ROOT / "include" / "gmgs.h"]
+    deps = [srcp] + list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + [ROOT / "include" / "gmgs.h", DEFAULT_STENCIL]
     if out.exists() and all(out.stat().st_mtime >= d.stat().st_mtime for d in deps):
         return out
     cmd = [nvcc(), *flags(debug), *FILE_FLAGS.get(src, []), "-c", str(srcp), "-o", str(out)]
@@ -69,6 +97,7 @@ def compile_one(src: str, debug: bool) -> Path:
 
 def build(debug: bool = False, jobs: int | None = None) -> Path:
     obj_dir(debug).mkdir(parents=True, exist_ok=True)
+    generate_default_stencil()
     srcs = [s for s in SOURCES if (CSRC / s).exists()]
     with cf.ThreadPoolExecutor(max_workers=jobs or min(8, len(srcs))) as ex:
         objs = list(ex.map(lambda s: compile_one(s, debug), srcs))

@@ -30,6 +30,7 @@
 // 1/64 of its FP32 rate: in FP64 the five operations per DOF of the state
 // update kept that pipe 53 % busy and the kernel at 2.41 ms on the 153M-DOF
 // model.)
+#include "element_host.h"
 #include "fine.cuh"
 
 namespace gmgs {
@@ -49,18 +50,8 @@ constexpr int RING = 4;
 // host: assembled interior stencil from the element matrix (row = output DOF)
 // ---------------------------------------------------------------------------
 void make_stencil(const double* ke_rows, Coef32& cf) {
-    double S[27][9] = {};
-    for (int k = 0; k < 27; ++k) {
-        const int dy = off_y(k), dx = off_x(k), dz = off_z(k);
-        for (int e = 0; e < 8; ++e) {
-            const int A = e & 1, B = (e >> 1) & 1, C = e >> 2;     // node = element origin + (A, B, C)
-            const int my = A + dy, mx = B + dx, mz = C + dz;       // neighbour relative to the origin
-            if (my < 0 || my > 1 || mx < 0 || mx > 1 || mz < 0 || mz > 1) continue;
-            const int cn = corner_of(A, B, C), cm = corner_of(my, mx, mz);
-            for (int a = 0; a < 3; ++a)
-                for (int b = 0; b < 3; ++b) S[k][3 * a + b] += ke_rows[(3 * cn + a) * 24 + 3 * cm + b];
-        }
-    }
+    double S[27][9];
+    stencil_from_rows(ke_rows, S);
     for (int k = 0; k < 27; ++k)
         for (int i = 0; i < 9; ++i) cf.S[k * 9 + i] = (float)S[k][i];
     for (int i = 0; i < KE; ++i) cf.K[i] = (float)ke_rows[i];
@@ -104,7 +95,7 @@ __device__ __forceinline__ void epi_fetch(const FineArgs& a, int S, int n, EpiDa
 // holds the state update's operands and keeps 80 registers (3 CTAs).
 // Measured on the 153M-DOF model: 5 CTAs/SM took the down-sweep from 1.16 to
 // 1.13 ms and the direction kernel from 1.26 to 1.22 ms against 4 CTAs/SM.
-template <int MODE>
+template <int MODE, bool DEF = false>
 __global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? 3 : 5)
     k_fine(FineLevel L, const __grid_constant__ Coef32 cf, FineArgs a, int zc) {
     __shared__ float ring[RING][3 * PLANE];
@@ -206,10 +197,10 @@ __global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? 3 : 5)
             epi_fetch<MODE>(a, S, n, ed);       // in flight during the stencil arithmetic
             float y[3];
             if (f & NF_INTERIOR) {
-                interior_s<RP, PLANE>(cf, P0, P1, P2, pc, y[0], y[1], y[2]);
+                interior_s<RP, PLANE, DEF>(cf, P0, P1, P2, pc, y[0], y[1], y[2]);
                 y[0] *= L.kscale; y[1] *= L.kscale; y[2] *= L.kscale;
             } else {
-                boundary_s<RP, PLANE>(L, cf, e8, n, P0, P1, P2, pc, y[0], y[1], y[2]);
+                boundary_s<RP, PLANE, DEF>(L, cf, e8, n, P0, P1, P2, pc, y[0], y[1], y[2]);
             }
             if (f & NF_FIX_X) y[0] = 0.f;
             if (f & NF_FIX_Y) y[1] = 0.f;
@@ -272,11 +263,23 @@ int fine_grid_blocks(const Grid& g) {
     return ((g.ny + 1 + TY - 1) / TY) * ((g.nx + 1 + TX - 1) / TX) * ((g.nz + 1 + 3) / 4);
 }
 
+// true when cf holds exactly the compiled-in default-material tables (then
+// the kernels with the coefficients as immediates give the same results)
+static bool coef_is_default(const Coef32& cf) {
+    for (int i = 0; i < 27 * 9; ++i)
+        if (cf.S[i] != dflt::S(i) || std::signbit(cf.S[i]) != std::signbit(dflt::S(i))) return false;
+    for (int i = 0; i < KE; ++i)
+        if (cf.K[i] != dflt::K(i) || std::signbit(cf.K[i]) != std::signbit(dflt::K(i))) return false;
+    const char* e = std::getenv("GMGS_DEFAULT_STENCIL");
+    return !(e && e[0] == '0');
+}
+
 template <int MODE>
 void launch_fine(Ctx& c, const FineLevel& L, const Coef32& cf, const FineArgs& a) {
     const int zc = pick_zc(L.g, c);
     dim3 grid((L.g.ny + 1 + TY - 1) / TY, (L.g.nx + 1 + TX - 1) / TX, (L.g.nz + 1 + zc - 1) / zc);
-    k_fine<MODE><<<grid, dim3(TY, TX, 1), 0, c.stream>>>(L, cf, a, zc);
+    if (coef_is_default(cf)) k_fine<MODE, true><<<grid, dim3(TY, TX, 1), 0, c.stream>>>(L, cf, a, zc);
+    else k_fine<MODE, false><<<grid, dim3(TY, TX, 1), 0, c.stream>>>(L, cf, a, zc);
     GMGS_LAUNCHED(c);
 }
 template void launch_fine<FM_PLAIN>(Ctx&, const FineLevel&, const Coef32&, const FineArgs&);

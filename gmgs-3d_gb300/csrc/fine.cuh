@@ -2,6 +2,7 @@
 #pragma once
 
 #include "gmgs_internal.cuh"
+#include "gmgs_default_stencil.h"   // generated at build time (build.py)
 
 namespace gmgs {
 
@@ -154,7 +155,9 @@ __device__ __forceinline__ void field_at(const FineArgs& a, int S, int s, float 
 // stencil arithmetic on the shared-memory ring
 // ---------------------------------------------------------------------------
 // interior node, second-difference form; P0, P1, P2 = planes z-1, z, z+1
-template <int RP, int PLANE>
+// DEF: the coefficients are the compiled-in default-material tables (dflt::S,
+// dflt::K: instruction immediates) instead of the kernel parameter cf
+template <int RP, int PLANE, bool DEF = false>
 __device__ __forceinline__ void interior_s(const Coef32& cf, const float* __restrict__ P0, const float* __restrict__ P1,
                                            const float* __restrict__ P2, int p, float& y0, float& y1, float& y2) {
     constexpr long long R = 3 * PLANE;   // one ring slot
@@ -177,14 +180,14 @@ __device__ __forceinline__ void interior_s(const Coef32& cf, const float* __rest
         for (int a = 0; a < 3; ++a)
 #pragma unroll
             for (int b = 0; b < 3; ++b)
-                if (s_nonzero(k, a, b)) acc[a] = fmaf(cf.S[k * 9 + 3 * a + b], d[b], acc[a]);
+                if (s_nonzero(k, a, b)) acc[a] = fmaf(DEF ? dflt::S(k * 9 + 3 * a + b) : cf.S[k * 9 + 3 * a + b], d[b], acc[a]);
     }
     y0 = acc[0]; y1 = acc[1]; y2 = acc[2];
 }
 
 // rows of one element (node at corner CI of the element with origin offset
 // (A, B, C)), first-difference form, coefficients K (row = output DOF) * s
-template <int RP, int PLANE, int A, int B, int C, bool PARAM>
+template <int RP, int PLANE, int A, int B, int C, bool PARAM, bool DEF = false>
 __device__ __forceinline__ void elem_rows(const Coef32& cf, const float* __restrict__ Kg, float s,
                                           const float* __restrict__ P0, const float* __restrict__ P1,
                                           const float* __restrict__ P2, int p, float c0, float c1, float c2,
@@ -203,7 +206,9 @@ __device__ __forceinline__ void elem_rows(const Coef32& cf, const float* __restr
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
             const int r = (3 * CI + a) * 24 + 3 * j;
-            if (PARAM) {
+            if (PARAM && DEF) {
+                t[a] = fmaf(dflt::K(r + 2), d2, fmaf(dflt::K(r + 1), d1, dflt::K(r) * d0));
+            } else if (PARAM) {
                 t[a] = fmaf(cf.K[r + 2], d2, fmaf(cf.K[r + 1], d1, cf.K[r] * d0));
             } else {
                 t[a] = fmaf(Kg[r + 2], d2, fmaf(Kg[r + 1], d1, Kg[r] * d0));
@@ -215,7 +220,7 @@ __device__ __forceinline__ void elem_rows(const Coef32& cf, const float* __restr
     }
 }
 
-template <int RP, int PLANE, int E>
+template <int RP, int PLANE, int E, bool DEF = false>
 __device__ __forceinline__ void boundary_elem(const FineLevel& L, const Coef32& cf, uint32_t e8, int n,
                                               const float* __restrict__ P0, const float* __restrict__ P1,
                                               const float* __restrict__ P2, int p, float c0, float c1, float c2,
@@ -234,10 +239,10 @@ __device__ __forceinline__ void boundary_elem(const FineLevel& L, const Coef32& 
         }
     }
     if (L.escale) s *= chk::ld(L.escale, es, L.g.slots, chk::FINE_ELEM);
-    elem_rows<RP, PLANE, A, B, C, true>(cf, nullptr, s, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);
+    elem_rows<RP, PLANE, A, B, C, true, DEF>(cf, nullptr, s, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);
 }
 
-template <int RP, int PLANE>
+template <int RP, int PLANE, bool DEF = false>
 __device__ __forceinline__ void boundary_s(const FineLevel& L, const Coef32& cf, uint32_t e8, int n,
                                            const float* __restrict__ P0, const float* __restrict__ P1,
                                            const float* __restrict__ P2, int p, float& y0, float& y1, float& y2) {
@@ -245,14 +250,14 @@ __device__ __forceinline__ void boundary_s(const FineLevel& L, const Coef32& cf,
     const float c0 = chk::ld(P1, p, R, chk::FINE_RING), c1 = chk::ld(P1, p + PLANE, R, chk::FINE_RING),
                 c2 = chk::ld(P1, p + 2 * PLANE, R, chk::FINE_RING);
     y0 = y1 = y2 = 0.f;
-    boundary_elem<RP, PLANE, 0>(L, cf, e8, n, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);
-    boundary_elem<RP, PLANE, 1>(L, cf, e8, n, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);
-    boundary_elem<RP, PLANE, 2>(L, cf, e8, n, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);
-    boundary_elem<RP, PLANE, 3>(L, cf, e8, n, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);
-    boundary_elem<RP, PLANE, 4>(L, cf, e8, n, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);
-    boundary_elem<RP, PLANE, 5>(L, cf, e8, n, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);
-    boundary_elem<RP, PLANE, 6>(L, cf, e8, n, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);
-    boundary_elem<RP, PLANE, 7>(L, cf, e8, n, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);
+    boundary_elem<RP, PLANE, 0, DEF>(L, cf, e8, n, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);
+    boundary_elem<RP, PLANE, 1, DEF>(L, cf, e8, n, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);
+    boundary_elem<RP, PLANE, 2, DEF>(L, cf, e8, n, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);
+    boundary_elem<RP, PLANE, 3, DEF>(L, cf, e8, n, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);
+    boundary_elem<RP, PLANE, 4, DEF>(L, cf, e8, n, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);
+    boundary_elem<RP, PLANE, 5, DEF>(L, cf, e8, n, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);
+    boundary_elem<RP, PLANE, 6, DEF>(L, cf, e8, n, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);
+    boundary_elem<RP, PLANE, 7, DEF>(L, cf, e8, n, P0, P1, P2, p, c0, c1, c2, y0, y1, y2);
 }
 
 

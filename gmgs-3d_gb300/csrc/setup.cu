@@ -494,22 +494,22 @@ __global__ void k_set_loads(int64_t n, const double* __restrict__ loads, const i
     }
 }
 // coarse fixed DOFs: restricted indicator != 0 (SetupSolver.m:247-254)
-__global__ void k_fixed_from_indicator(int64_t S, const double* __restrict__ ind, uint8_t* __restrict__ f) {
+__global__ void k_fixed_from_indicator(int64_t S, const float* __restrict__ ind, uint8_t* __restrict__ f) {
     GRID_STRIDE(s, S) {
         uint8_t v = f[s] & NF_KEEP;
         if (v & NF_SOLID) {
-            if (ind[s] != 0.0) v |= NF_FIX_X;
-            if (ind[s + S] != 0.0) v |= NF_FIX_Y;
-            if (ind[s + 2 * S] != 0.0) v |= NF_FIX_Z;
+            if (ind[s] != 0.f) v |= NF_FIX_X;
+            if (ind[s + S] != 0.f) v |= NF_FIX_Y;
+            if (ind[s + 2 * S] != 0.f) v |= NF_FIX_Z;
         }
         f[s] = v;
     }
 }
-__global__ void k_indicator(int64_t S, const uint8_t* __restrict__ f, double* __restrict__ ind) {
+__global__ void k_indicator(int64_t S, const uint8_t* __restrict__ f, float* __restrict__ ind) {
     GRID_STRIDE(s, S) {
-        ind[s] = (f[s] & NF_FIX_X) ? 1.0 : 0.0;
-        ind[s + S] = (f[s] & NF_FIX_Y) ? 1.0 : 0.0;
-        ind[s + 2 * S] = (f[s] & NF_FIX_Z) ? 1.0 : 0.0;
+        ind[s] = (f[s] & NF_FIX_X) ? 1.f : 0.f;
+        ind[s + S] = (f[s] & NF_FIX_Y) ? 1.f : 0.f;
+        ind[s + 2 * S] = (f[s] & NF_FIX_Z) ? 1.f : 0.f;
     }
 }
 
@@ -966,17 +966,20 @@ void build_coarse_bc(Model& M, const std::function<void()>& overlap) {
     Ctx& c = M.ctx;
     const int L = M.num_levels;
     // restricted fixed indicator, level by level (SetupSolver.m:247-254)
-    DevBuf ind = dalloc(3 * M.levels[0].g.slots * sizeof(double));
+    // the indicator in FP32: its restrictions sum non-negative terms (0/1 values
+    // times the weights 1, 1/2, 1/4, 1/8), so a coarse entry is nonzero exactly
+    // when one of its terms is, in FP32 as in FP64; only that test is used
+    DevBuf ind = dalloc(3 * M.levels[0].g.slots * sizeof(float));
     k_indicator<<<blocks_for(c, M.levels[0].g.slots), 256, 0, c.stream>>>(
-        M.levels[0].g.slots, M.levels[0].nflag.as<uint8_t>(), ind.as<double>());
+        M.levels[0].g.slots, M.levels[0].nflag.as<uint8_t>(), ind.as<float>());
     GMGS_LAUNCHED(c);
     for (int l = 1; l < L; ++l) {
         Level& lv = M.levels[l];
-        DevBuf indc = dalloc(3 * lv.g.slots * sizeof(double));
-        GMGS_CUDA(cudaMemsetAsync(indc.p, 0, 3 * lv.g.slots * sizeof(double), c.stream));
-        launch_restrict<double>(c, M.levels[l - 1].g, lv.g, lv.nflag.as<uint8_t>(), ind.as<double>(),
-                                indc.as<double>());
-        k_fixed_from_indicator<<<blocks_for(c, lv.g.slots), 256, 0, c.stream>>>(lv.g.slots, indc.as<double>(),
+        DevBuf indc = dalloc(3 * lv.g.slots * sizeof(float));
+        GMGS_CUDA(cudaMemsetAsync(indc.p, 0, 3 * lv.g.slots * sizeof(float), c.stream));
+        launch_restrict<float>(c, M.levels[l - 1].g, lv.g, lv.nflag.as<uint8_t>(), ind.as<float>(),
+                               indc.as<float>());
+        k_fixed_from_indicator<<<blocks_for(c, lv.g.slots), 256, 0, c.stream>>>(lv.g.slots, indc.as<float>(),
                                                                                  lv.nflag.as<uint8_t>());
         GMGS_LAUNCHED(c);
         GMGS_CUDA(cudaStreamSynchronize(c.stream));

@@ -30,8 +30,11 @@
 // 1/64 of its FP32 rate: in FP64 the five operations per DOF of the state
 // update kept that pipe 53 % busy and the kernel at 2.41 ms on the 153M-DOF
 // model.)
+#include <cstring>
+
 #include "element_host.h"
 #include "fine.cuh"
+#include "tcgen05.cuh"
 
 namespace gmgs {
 
@@ -91,13 +94,61 @@ __device__ __forceinline__ void epi_fetch(const FineArgs& a, int S, int n, EpiDa
     }
 }
 
+// --- TMA staging of the CG update's per-node operands ------------------------
+// One tile plane of one array (32 y x 8 x, three components) is a 3 KB box;
+// the six arrays of a plane make one 18 KB stage in dynamic shared memory.
+// The boxes are written with the 128-byte swizzle: the 16-byte chunk index
+// (address bits 4-6) is XORed with the 128-byte row index (bits 7-9), and a
+// row here is one x column of 32 y values, so the stage base is aligned to
+// 1024 bytes and node (ly, lx) of component c sits at float
+//   c * 256 + 32 * lx + ((((ly >> 2) ^ lx) << 2) | (ly & 3)).
+constexpr int EPI_BOX = 3 * NT;                              // floats per array and plane
+constexpr int EPI_STAGE_BYTES = EPI_ARRAYS * EPI_BOX * 4;
+constexpr size_t EPI_DYN_SMEM = EPI_STAGE_BYTES + 1024;      // + alignment slack
+constexpr uint64_t EPI_WAIT_NS = 5000000ull;                 // a plane's copies take microseconds
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* mbar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tc::smem_u32(mbar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_cta() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+// box at (y slot index, x slot index, z slot index, component 0) of a tensor map
+__device__ __forceinline__ void tma_load_plane(float* dst, const CUtensorMap* map, int sy, int sx, int sz,
+                                               uint64_t* mbar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+        "%5}], [%6];" ::"r"(tc::smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(sy), "r"(sx), "r"(sz), "r"(0), "r"(tc::smem_u32(mbar))
+        : "memory");
+}
+__device__ __forceinline__ void epi_from_stage(const float* st, int sidx, bool first, EpiData& d) {
+    constexpr long long N = EPI_ARRAYS * EPI_BOX;
+    constexpr int R = chk::FINE_RING;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const int i = c * NT + sidx;
+        d.r[c] = chk::ld(st, i, N, R);
+        d.rl[c] = chk::ld(st, EPI_BOX + i, N, R);
+        d.xh[c] = chk::ld(st, 2 * EPI_BOX + i, N, R);
+        d.xl[c] = chk::ld(st, 3 * EPI_BOX + i, N, R);
+        if (!first) {
+            d.q[c] = chk::ld(st, 4 * EPI_BOX + i, N, R);
+            d.pp[c] = chk::ld(st, 5 * EPI_BOX + i, N, R);
+        }
+    }
+}
+
 // 48 registers (5 CTAs per SM) for the stencil-only modes; the CG update
-// holds the state update's operands and keeps 80 registers (3 CTAs).
+// holds the state update's operands and keeps 80 registers (3 CTAs), or,
+// with the operands staged by TMA (TMA = true), 64 registers (4 CTAs).
 // Measured on the 153M-DOF model: 5 CTAs/SM took the down-sweep from 1.16 to
 // 1.13 ms and the direction kernel from 1.26 to 1.22 ms against 4 CTAs/SM.
-template <int MODE, bool DEF = false>
-__global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? 3 : 5)
-    k_fine(FineLevel L, const __grid_constant__ Coef32 cf, FineArgs a, int zc) {
+template <int MODE, bool DEF = false, bool TMA = false>
+__global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? (TMA ? 4 : 3) : 5)
+    k_fine(FineLevel L, const __grid_constant__ Coef32 cf, FineArgs a, int zc, const __grid_constant__ EpiMaps em) {
+    static_assert(!TMA || MODE == FM_CG_UPDATE_JACOBI, "operand staging is for the CG update");
     __shared__ float ring[RING][3 * PLANE];
     __shared__ double sh[32];
     const Grid& g = L.g;
@@ -119,6 +170,26 @@ __global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? 3 : 5)
     const int tid = threadIdx.x + threadIdx.y * TY;
     const int wrp = tid >> 5, lane = tid & 31;
     const int ly = (wrp & 3) * 8 + (lane & 7), lx = (wrp >> 2) * 4 + (lane >> 3);
+
+    // TMA: the plane's six operand arrays go to a shared-memory stage, loaded by
+    // thread 0 at the top of the plane's step and read after the stencil
+    // arithmetic, so no registers hold them across it; the step's barrier
+    // orders the previous plane's reads before the next load
+    extern __shared__ unsigned char fine_dyn[];
+    __shared__ uint64_t ebar;
+    __shared__ int efail;
+    float* stage = nullptr;
+    int sidx = 0;
+    int last_phase = -1;      // thread 0: the last phase it armed
+    if constexpr (TMA) {
+        stage = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(fine_dyn) + 1023) & ~uintptr_t(1023));
+        sidx = 32 * lx + ((((ly >> 2) ^ lx) << 2) | (ly & 3));
+        if (tid == 0) {
+            tc::mbar_init(&ebar, 1);
+            efail = 0;
+            tc::mbar_fence_init();
+        }
+    }
 
     // beta = r.z / r_old.z_old, alpha = r.z / p.q: one FP64 division per CTA
     // instead of one per thread on GB300's narrow FP64 pipe
@@ -182,6 +253,24 @@ __global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? 3 : 5)
     for (int iz = zb; iz < ze; ++iz) {
         store(ring[(iz + 1) % RING], vc, vh);
         __syncthreads();
+        if constexpr (TMA) {
+            if (tid == 0 && !efail) {
+                // the previous plane's copies have landed long ago; waiting for
+                // them keeps one phase of the barrier in flight at a time
+                const int k = iz - zb;
+                if (k == 0 || tc::mbar_wait_bounded(&ebar, (k - 1) & 1, EPI_WAIT_NS)) {
+                    const int na = a.first ? 4 : EPI_ARRAYS;
+                    fence_proxy_async_cta();
+                    mbar_expect_tx(&ebar, (uint32_t)(na * EPI_BOX * 4));
+                    for (int j = 0; j < na; ++j)
+                        tma_load_plane(stage + j * EPI_BOX, &em.m[j], y0 + Grid::YOFF, x0 + 1, iz + 1, &ebar);
+                    last_phase = k;
+                } else {
+                    efail = 1;
+                    if (a.err) atomicExch(a.err, 1);
+                }
+            }
+        }
         if (iz + 2 <= g.nz + 1) fetch(iz + 2, vc, vh);
         const uint32_t f = f_next, e8 = e8_next;
         if (own && iz + 1 < ze) {
@@ -194,7 +283,7 @@ __global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? 3 : 5)
         if (own && (f & NF_SOLID) && !(f & NF_PEREL)) {
             const int n = cbase + iz * sz;
             EpiData ed;
-            epi_fetch<MODE>(a, S, n, ed);       // in flight during the stencil arithmetic
+            if constexpr (!TMA) epi_fetch<MODE>(a, S, n, ed);       // in flight during the stencil arithmetic
             float y[3];
             if (f & NF_INTERIOR) {
                 interior_s<RP, PLANE, DEF>(cf, P0, P1, P2, pc, y[0], y[1], y[2]);
@@ -205,6 +294,13 @@ __global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? 3 : 5)
             if (f & NF_FIX_X) y[0] = 0.f;
             if (f & NF_FIX_Y) y[1] = 0.f;
             if (f & NF_FIX_Z) y[2] = 0.f;
+            if constexpr (TMA) {
+                if (!efail && !tc::mbar_wait_bounded(&ebar, (iz - zb) & 1, EPI_WAIT_NS)) {
+                    efail = 1;
+                    if (a.err) atomicExch(a.err, 1);
+                }
+                epi_from_stage(stage, sidx, a.first, ed);
+            }
             const long long n3 = 3ll * S;
             constexpr int O = chk::FINE_OUT;
 #pragma unroll
@@ -243,6 +339,11 @@ __global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? 3 : 5)
             }
         }
     }
+    if constexpr (TMA) {
+        // no copy may still be in flight when the CTA's shared memory is released
+        // (every earlier phase completed before the next one was armed)
+        if (tid == 0 && last_phase >= 0) tc::mbar_wait_bounded(&ebar, last_phase & 1, EPI_WAIT_NS);
+    }
     if (MODE == FM_CG_DIRECTION || MODE == FM_CG_UPDATE_JACOBI) grid_dot_finish(dot.value(), a.dot, sh);
 }
 
@@ -274,12 +375,68 @@ static bool coef_is_default(const Coef32& cf) {
     return !(e && e[0] == '0');
 }
 
+// cuTensorMapEncodeTiled from the driver (the library links only the runtime)
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiledFn tensor_map_encoder() {
+    static const EncodeTiledFn fn = []() -> EncodeTiledFn {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        return reinterpret_cast<EncodeTiledFn>(p);
+    }();
+    return fn;
+}
+
+// (y, x, z, component) view of one dense-slot vector: strides py, py*px and
+// the component plane (all multiples of 32 bytes: py is a multiple of 8);
+// the box is one tile plane, and boxes over the grid edge read zeros
+static bool encode_plane_map(CUtensorMap* m, const Grid& g, const float* base) {
+    const EncodeTiledFn fn = tensor_map_encoder();
+    if (!fn || !base || (reinterpret_cast<uintptr_t>(base) & 15)) return false;
+    const cuuint64_t dim[4] = {(cuuint64_t)g.py, (cuuint64_t)g.px, (cuuint64_t)g.pz, 3};
+    const cuuint64_t stride[3] = {(cuuint64_t)g.py * 4, (cuuint64_t)g.py * g.px * 4, (cuuint64_t)g.slots * 4};
+    const cuuint32_t box[4] = {TY, TX, 1, 3};
+    const cuuint32_t es[4] = {1, 1, 1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<float*>(base), dim, stride, box, es,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// GMGS_EPI_TMA=0 keeps the CG update's operands in registers (per-thread
+// loads issued before the stencil arithmetic) instead of the TMA stage
+static bool epi_tma_enabled() {
+    const char* e = std::getenv("GMGS_EPI_TMA");
+    return !(e && e[0] == '0');
+}
+
 template <int MODE>
 void launch_fine(Ctx& c, const FineLevel& L, const Coef32& cf, const FineArgs& a) {
     const int zc = pick_zc(L.g, c);
     dim3 grid((L.g.ny + 1 + TY - 1) / TY, (L.g.nx + 1 + TX - 1) / TX, (L.g.nz + 1 + zc - 1) / zc);
-    if (coef_is_default(cf)) k_fine<MODE, true><<<grid, dim3(TY, TX, 1), 0, c.stream>>>(L, cf, a, zc);
-    else k_fine<MODE, false><<<grid, dim3(TY, TX, 1), 0, c.stream>>>(L, cf, a, zc);
+    const dim3 blk(TY, TX, 1);
+    const bool def = coef_is_default(cf);
+    EpiMaps em;
+    std::memset(&em, 0, sizeof(em));
+    if constexpr (MODE == FM_CG_UPDATE_JACOBI) {
+        const float* arr[EPI_ARRAYS] = {a.r32, a.r_lo, a.x_hi, a.x_lo, a.q32, a.pold};
+        bool tma = epi_tma_enabled();
+        for (int j = 0; j < EPI_ARRAYS && tma; ++j) tma = encode_plane_map(&em.m[j], L.g, arr[j]);
+        if (tma) {
+            if (def) k_fine<MODE, true, true><<<grid, blk, EPI_DYN_SMEM, c.stream>>>(L, cf, a, zc, em);
+            else k_fine<MODE, false, true><<<grid, blk, EPI_DYN_SMEM, c.stream>>>(L, cf, a, zc, em);
+            GMGS_LAUNCHED(c);
+            return;
+        }
+    }
+    if (def) k_fine<MODE, true><<<grid, blk, 0, c.stream>>>(L, cf, a, zc, em);
+    else k_fine<MODE, false><<<grid, blk, 0, c.stream>>>(L, cf, a, zc, em);
     GMGS_LAUNCHED(c);
 }
 template void launch_fine<FM_PLAIN>(Ctx&, const FineLevel&, const Coef32&, const FineArgs&);

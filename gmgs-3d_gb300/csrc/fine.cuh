@@ -1,6 +1,8 @@
 // Tiled FP32 operator kernels of the mixed-precision path (fine.cu).
 #pragma once
 
+#include <cuda.h>                   // CUtensorMap (types only; the encoder is fetched from the driver at run time)
+
 #include "gmgs_internal.cuh"
 #include "gmgs_default_stencil.h"   // generated at build time (build.py)
 
@@ -58,6 +60,15 @@ struct FineArgs {
     float* x_lo = nullptr;
     float* r32out = nullptr;         // high part of the updated residual (must not alias r32)
     DotOut dot;
+    int* err = nullptr;              // set when a bounded wait for staged operands ran out
+};
+
+// TMA descriptors of FM_CG_UPDATE_JACOBI's per-node operands (r high, r low,
+// x high, x low, q, p), each a (y, x, z, component) tensor over the dense
+// slot grid with a 32 x 8 x 1 x 3 box: one tile plane of all three components.
+constexpr int EPI_ARRAYS = 6;
+struct EpiMaps {
+    CUtensorMap m[EPI_ARRAYS];
 };
 
 

@@ -14,7 +14,7 @@
 
 namespace gmgs {
 
-enum { SC_RZ0 = 0, SC_RZ1 = 1, SC_PQ = 2, SC_RR = 3, SC_BB = 4, SC_TC = 5, SC_N = 8 };   // SC_TC: host copy of the tensor-core error flag
+enum { SC_RZ0 = 0, SC_RZ1 = 1, SC_PQ = 2, SC_RR = 3, SC_BB = 4, SC_TC = 5, SC_N = 8 };   // SC_TC: host copy of the device wait-error flag
 
 static void zalloc(Ctx& c, DevBuf& b, size_t bytes) {
     if (b.bytes < bytes) b = dalloc(bytes);
@@ -97,16 +97,18 @@ static bool tc_enabled() {
     return e && e[0] == '1';
 }
 
-// A tensor-core kernel whose wait on its MMA ran out sets the device flag;
-// the solve reports it instead of returning a result computed without it.
+// A kernel whose bounded wait ran out (a tensor-core kernel waiting for its
+// MMA, or the CG update waiting for its TMA-staged operands) sets the device
+// flag; the solve reports it instead of returning a result computed without
+// the data it waited for.
 static void check_tc(Model& M) {
-    if (!M.use_tc || !M.tc_err.p) return;
+    if (!M.tc_err.p) return;
     int flag = 0;
     GMGS_CUDA(cudaMemcpyAsync(&flag, M.tc_err.p, sizeof(int), cudaMemcpyDeviceToHost, M.ctx.stream));
     GMGS_CUDA(cudaStreamSynchronize(M.ctx.stream));
     if (flag) {
         GMGS_CUDA(cudaMemsetAsync(M.tc_err.p, 0, sizeof(int), M.ctx.stream));
-        throw Error(GMGS_ERR_CUDA, "a tensor-core kernel's wait for its MMA timed out");
+        throw Error(GMGS_ERR_CUDA, "a kernel's bounded wait for its tensor-core MMA or staged operands timed out");
     }
 }
 
@@ -367,6 +369,7 @@ static int pcg_mixed(Model& M, const double* b, double* x, int32_t* iters_out, d
         a.cur = cur;
         a.first = first;
         a.dot = dot_out(M, SC_RR);
+        a.err = M.tc_err.as<int>();
         c.mark(PK_FINE_MATVEC, false);
         c.mark(PK_UPDATE_JACOBI, false);
         launch_l0<FM_CG_UPDATE_JACOBI>(M, f0, a);
@@ -437,10 +440,9 @@ static int pcg_mixed(Model& M, const double* b, double* x, int32_t* iters_out, d
         c.mark(PK_CG_ITER, true);
         GMGS_CUDA(cudaMemcpyAsync(M.scal_host + SC_RR, scal + SC_RR, sizeof(double), cudaMemcpyDeviceToHost,
                                   c.stream));
-        if (M.use_tc)
-            GMGS_CUDA(cudaMemcpyAsync(M.scal_host + SC_TC, M.tc_err.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+        GMGS_CUDA(cudaMemcpyAsync(M.scal_host + SC_TC, M.tc_err.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
         GMGS_CUDA(cudaStreamSynchronize(c.stream));
-        if (M.use_tc && *reinterpret_cast<const int*>(M.scal_host + SC_TC)) break;   // check_tc reports it
+        if (*reinterpret_cast<const int*>(M.scal_host + SC_TC)) break;   // check_tc reports it
         resnorm = std::sqrt(M.scal_host[SC_RR]) / normB;
         if (M.prm.verbose) std::printf(" It.: %4d Res.: %16.6e\n", its, resnorm);
         if (!std::isfinite(resnorm)) {

@@ -142,7 +142,8 @@ __device__ __forceinline__ void epi_from_stage(const float* st, int sidx, bool f
 
 // 48 registers (5 CTAs per SM) for the stencil-only modes; the CG update
 // holds the state update's operands and keeps 80 registers (3 CTAs), or,
-// with the operands staged by TMA (TMA = true), 64 registers (4 CTAs).
+// with the operands staged by TMA (TMA = true), 64 registers (4 CTAs; 5 CTAs
+// at 48 registers spilled and took 2.31 ms against 1.86 ms).
 // Measured on the 153M-DOF model: 5 CTAs/SM took the down-sweep from 1.16 to
 // 1.13 ms and the direction kernel from 1.26 to 1.22 ms against 4 CTAs/SM.
 template <int MODE, bool DEF = false, bool TMA = false>
@@ -280,7 +281,8 @@ __global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? (TMA ? 4 : 3
         const float* P0 = ring[(iz - 1 + RING) % RING];
         const float* P1 = ring[iz % RING];
         const float* P2 = ring[(iz + 1) % RING];
-        if (own && (f & NF_SOLID) && !(f & NF_PEREL)) {
+        const bool node = own && (f & NF_SOLID) && !(f & NF_PEREL);
+        if (node) {
             const int n = cbase + iz * sz;
             EpiData ed;
             if constexpr (!TMA) epi_fetch<MODE>(a, S, n, ed);       // in flight during the stencil arithmetic
@@ -330,12 +332,21 @@ __global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? (TMA ? 4 : 3
                     chk::st(a.x_lo, i, n3, O, xl);
                     chk::st(a.r_lo, i, n3, O, rl);
                     chk::st(a.r32out, i, n3, O, rh);
-                    dot.add(rm32 * rm32);
+                    dot.add(__fmul_rn(rm32, rm32));
                 } else {
                     chk::st(a.pout, i, n3, O, v);
                     chk::st(a.out32, i, n3, O, y[b]);                   // q = A p
-                    dot.add(v * y[b]);
+                    dot.add(__fmul_rn(v, y[b]));
                 }
+            }
+        }
+        if constexpr (TMA) {
+            // every thread sees each phase complete within its step, so no
+            // thread's wait in the next step can meet this phase still pending
+            // (a parity wait cannot tell phase k from phase k + 2)
+            if (!node && !efail && !tc::mbar_wait_bounded(&ebar, (iz - zb) & 1, EPI_WAIT_NS)) {
+                efail = 1;
+                if (a.err) atomicExch(a.err, 1);
             }
         }
     }
@@ -396,7 +407,8 @@ static EncodeTiledFn tensor_map_encoder() {
 
 // (y, x, z, component) view of one dense-slot vector: strides py, py*px and
 // the component plane (all multiples of 32 bytes: py is a multiple of 8);
-// the box is one tile plane, and boxes over the grid edge read zeros
+// the box is one tile plane, and boxes over the grid edge read zeros; the
+// 128-byte swizzle spreads the stage's 8 x 4 node patches over the banks
 static bool encode_plane_map(CUtensorMap* m, const Grid& g, const float* base) {
     const EncodeTiledFn fn = tensor_map_encoder();
     if (!fn || !base || (reinterpret_cast<uintptr_t>(base) & 15)) return false;
@@ -456,6 +468,12 @@ template void launch_fine<FM_CG_DIRECTION>(Ctx&, const FineLevel&, const Coef32&
 // computed, and only solid nodes are written.  The four coarse values of a
 // coarse plane (Iy + {0,1}, Ix + {0,1}) stay in registers for the two fine
 // planes that use them (in-bounds: the halo covers Iy + 1, Ix + 1, Iz + 1).
+// z = w r + P z_c + w r' (Vcycle.m:27-32 with the stale residual r'), each
+// rounding explicit so that every kernel forming it gives the same bits
+__device__ __forceinline__ float up_post(float w, float r, float rp, float wp, float t) {
+    return __fadd_rn(fmaf(w, r, __fmul_rn(wp, t)), __fmul_rn(w, rp));
+}
+
 template <bool DOT>
 __global__ void __launch_bounds__(256, 4) k_up32(Grid gf, Grid gc, const uint8_t* __restrict__ nflag,
                                               const uint8_t* __restrict__ tile_occ, int zc,
@@ -530,10 +548,10 @@ __global__ void __launch_bounds__(256, 4) k_up32(Grid gf, Grid gc, const uint8_t
                         t += (oz & oy) ? qb[c][1] : 0.f;
                         t += (oz & ox) ? qb[c][2] : 0.f;
                         t += (oz & ox & oy) ? qb[c][3] : 0.f;
-                        float out = (wdc[c] * rc[c] + w * t) + wdc[c] * rpc[c];
+                        float out = up_post(wdc[c], rc[c], rpc[c], w, t);
                         if (zero_fixed && (flc & (NF_FIX_X << c))) out = 0.f;
                         chk::st(xf, fs + c * Sf, 3ll * Sf, chk::UP_OUT, out);
-                        if (DOT) dot.add(rc[c] * out);
+                        if (DOT) dot.add(__fmul_rn(rc[c], out));
                     }
                 }
                 if (oz) {

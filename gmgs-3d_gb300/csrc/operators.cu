@@ -339,6 +339,22 @@ template void launch_copy<double, double>(Ctx&, int64_t, double*, const double*)
 // 27 fine nodes around coarse node C, w = prod(1 - |d|/2); its interpolation
 // equals the trilinear interpolant restricted to solid fine nodes.
 // ---------------------------------------------------------------------------
+// one line of the restriction stencil, (w/2 a + b) + w/2 c with w = 1, and one
+// weighted accumulation (weight 1 when `centre`, else 1/2); the roundings are
+// explicit so that every kernel summing in this order gives the same bits
+__device__ __forceinline__ float restrict_line(float a, float b, float c) {
+    return __fmaf_rn(0.5f, c, __fmaf_rn(0.5f, a, b));
+}
+__device__ __forceinline__ double restrict_line(double a, double b, double c) {
+    return __fma_rn(0.5, c, __fma_rn(0.5, a, b));
+}
+__device__ __forceinline__ float restrict_acc(float acc, float v, bool centre) {
+    return centre ? __fadd_rn(acc, v) : __fmaf_rn(0.5f, v, acc);
+}
+__device__ __forceinline__ double restrict_acc(double acc, double v, bool centre) {
+    return centre ? __dadd_rn(acc, v) : __fma_rn(0.5, v, acc);
+}
+
 template <typename T>
 __global__ void k_restrict(Grid gf, Grid gc, const uint8_t* __restrict__ nflag_c, const T* __restrict__ rf,
                            T* __restrict__ rc) {
@@ -365,11 +381,11 @@ __global__ void k_restrict(Grid gf, Grid gc, const uint8_t* __restrict__ nflag_c
 #pragma unroll
             for (int b = -1; b <= 1; ++b) {
                 const int64_t s = comp * Sf + f0 + b * sx + c * sz;
-                const T line = (T)0.5 * chk::ld(rf, s - 1, 3 * Sf, R) + chk::ld(rf, s, 3 * Sf, R) +
-                               (T)0.5 * chk::ld(rf, s + 1, 3 * Sf, R);
-                accx += (b == 0 ? (T)1 : (T)0.5) * line;
+                const T line = restrict_line(chk::ld(rf, s - 1, 3 * Sf, R), chk::ld(rf, s, 3 * Sf, R),
+                                             chk::ld(rf, s + 1, 3 * Sf, R));
+                accx = restrict_acc(accx, line, b == 0);
             }
-            accz += (c == 0 ? (T)1 : (T)0.5) * accx;
+            accz = restrict_acc(accz, accx, c == 0);
         }
         chk::st(rc, cs + comp * Sc, 3 * Sc, R, accz);
     }

@@ -1,13 +1,13 @@
-"""The CG update kernel with its per-node operands (r high and low, x high
-and low, q, p) staged into shared memory by TMA (fine.cu, k_fine<2, DEF,
-true>: one 32 x 8 x 3 box per array and plane, 128-byte swizzle, an mbarrier
-per CTA) against the same kernel loading them into registers
-(GMGS_EPI_TMA=0).
+"""The CG update kernel of the mixed path with its per-node operands (r and
+x, high and low parts, q, p) staged into shared memory by TMA (fine.cu,
+k_fine<2, DEF, true>: one 32 x 8 x 3 box per array and plane, 128-byte
+swizzle, one mbarrier phase per plane) against the same kernel loading them
+into registers (GMGS_EPI_TMA=0).
 
-Both read the same values and run the same FP32 arithmetic, so the mixed
-solve is bit-identical; the models have ragged extents (boxes that reach past
-the grid's edge read zeros), coarse levels with per-element matrices and a
-density field.
+Both read the same values and round the same operations in the same order,
+so the mixed solve is bit-identical; the models have ragged extents (boxes
+that reach past the grid's edge read zeros), coarse levels with per-element
+matrices and a density field.
 """
 import numpy as np
 import pytest
@@ -41,9 +41,12 @@ def test_tma_staged_update_bit_identical(name, monkeypatch):
     build, L, rr = CASES[name]
     vox = build()
     rho = synthetic.density(int(vox.sum()), rr, 5) if rr else None
-    monkeypatch.setenv("GMGS_EPI_TMA", "0")
+    switches = ("GMGS_EPI_TMA",)
+    for k in switches:
+        monkeypatch.setenv(k, "0")
     u0, it0, r0 = _solve(vox, L, rho)
-    monkeypatch.delenv("GMGS_EPI_TMA")
+    for k in switches:
+        monkeypatch.delenv(k)
     u1, it1, r1 = _solve(vox, L, rho)
     assert it1 == it0
     assert r1 == r0

@@ -6,8 +6,9 @@ into registers (GMGS_EPI_TMA=0).
 
 Both read the same values and round the same operations in the same order,
 so the mixed solve is bit-identical; the models have ragged extents (boxes
-that reach past the grid's edge read zeros), coarse levels with per-element
-matrices and a density field.
+that reach past the grid's edge read zeros), tile planes without a node to
+update inside a CTA's z-chunk, coarse levels with per-element matrices and a
+density field.
 """
 import numpy as np
 import pytest
@@ -16,7 +17,17 @@ from gmgs import Solver, synthetic
 
 pytestmark = pytest.mark.gpu
 
+def _stepped():
+    """A block whose upper half keeps only a slab x < 9: the column tiles over
+    x >= 9 have solid nodes in their lower planes and none above, so a CTA's
+    z-chunk holds planes where no thread has a node to update."""
+    vox = np.ones((20, 30, 40), dtype=np.int32)     # (y, x, z)
+    vox[:, 9:, 20:] = 0
+    return np.asfortranarray(vox)
+
+
 CASES = {
+    "stepped_L3": (_stepped, 3, None),
     "ragged_L3": (lambda: synthetic.sphere_voids(21, 13, 18, 6, 7), 3, None),
     "block42_L5": (lambda: synthetic.make("block42_fp64")[0], 5, None),
     "density_L3": (lambda: synthetic.sphere_voids(28, 24, 32, 2, 5), 3, (0.3, 1.0)),

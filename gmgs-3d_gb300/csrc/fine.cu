@@ -110,6 +110,17 @@ constexpr uint64_t EPI_WAIT_NS = 5000000ull;                 // a plane's copies
 // halo points (threads 0..83 do), so the copies do not lengthen the warp the
 // plane's barrier waits for (measured 1.854 -> 1.835 ms against thread 0)
 constexpr int EPI_ISSUER = NT - 32;
+// The field stage: the mode's field inputs of one plane with the one-node
+// halo, a 40 (y, from y0 - 4) x 10 (x, from x0 - 1) x 3 box per array,
+// unswizzled (a warp reads an 8 x 4 node patch at row pitch 40, like the
+// ring), each array padded to a multiple of 128 bytes.  Ring point p (pitch
+// RP = 40, from y0 - 1) is box element p + 3.
+constexpr int FLD_BOX = 3 * PLANE;                            // 1200 floats
+constexpr int FLD_PITCH = (FLD_BOX * 4 + 127) / 128 * 32;     // 1216 floats
+static_assert(RP == 40 && HX == 10, "the field box and the ring share their pitch");
+__host__ __device__ constexpr int field_arrays(int mode) {
+    return mode == FM_PLAIN ? 1 : (mode == FM_CG_UPDATE_JACOBI ? 3 : 2);
+}
 
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* mbar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tc::smem_u32(mbar)), "r"(bytes)
@@ -150,9 +161,12 @@ __device__ __forceinline__ void epi_from_stage(const float* st, int sidx, bool f
 // at 48 registers spilled and took 2.31 ms against 1.86 ms).
 // Measured on the 153M-DOF model: 5 CTAs/SM took the down-sweep from 1.16 to
 // 1.13 ms and the direction kernel from 1.26 to 1.22 ms against 4 CTAs/SM.
-template <int MODE, bool DEF = false, bool TMA = false>
-__global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? (TMA ? 4 : 3) : 5)
+// STG bit 0: the CG update's operands staged by TMA; bit 1: the field inputs
+// staged by TMA (else loaded per thread into registers one plane ahead)
+template <int MODE, bool DEF = false, int STG = 0>
+__global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? ((STG & 1) ? 4 : 3) : 5)
     k_fine(FineLevel L, const __grid_constant__ Coef32 cf, FineArgs a, int zc, const __grid_constant__ EpiMaps em) {
+    constexpr bool TMA = (STG & 1) != 0, FTMA = (STG & 2) != 0;
     static_assert(!TMA || MODE == FM_CG_UPDATE_JACOBI, "operand staging is for the CG update");
     __shared__ float ring[RING][3 * PLANE];
     __shared__ double sh[32];
@@ -181,16 +195,24 @@ __global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? (TMA ? 4 : 3
     // arithmetic, so no registers hold them across it; the step's barrier
     // orders the previous plane's reads before the next load
     extern __shared__ unsigned char fine_dyn[];
-    __shared__ uint64_t ebar;
+    __shared__ uint64_t ebar, fbar;
     __shared__ int efail;
     float* stage = nullptr;
+    float* fstage = nullptr;
     int sidx = 0;
     int last_phase = -1;      // EPI_ISSUER: the last phase it armed
     if constexpr (TMA) {
         stage = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(fine_dyn) + 1023) & ~uintptr_t(1023));
         sidx = 32 * lx + ((((ly >> 2) ^ lx) << 2) | (ly & 3));
+    }
+    if constexpr (FTMA) {
+        fstage = TMA ? stage + EPI_ARRAYS * EPI_BOX
+                     : reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(fine_dyn) + 127) & ~uintptr_t(127));
+    }
+    if constexpr (TMA || FTMA) {
         if (tid == 0) {
-            tc::mbar_init(&ebar, 1);
+            if (TMA) tc::mbar_init(&ebar, 1);
+            if (FTMA) tc::mbar_init(&fbar, 1);
             efail = 0;
             tc::mbar_fence_init();
         }
@@ -254,10 +276,58 @@ __global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? (TMA ? 4 : 3
         e8_next = chk::ld(L.emask8, cbase + zb * sz, g.slots, chk::FINE_FLAGS);
     }
     Kahan dot;
+    // FTMA: the field of plane z from the field stage (ring point p is box element p + 3)
+    int nfa = field_arrays(MODE);                 // the first CG iteration has no q / p term
+    if (a.first && (MODE == FM_CG_DIRECTION || MODE == FM_CG_UPDATE_JACOBI)) --nfa;
+    auto form = [&](int p, float v[3]) {
+        constexpr long long N = field_arrays(MODE) * FLD_PITCH;
+        constexpr int R = chk::FINE_RING;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const int i = c * PLANE + p + 3;
+            const float f0 = chk::ld(fstage, i, N, R);
+            if (MODE == FM_PLAIN) {
+                v[c] = f0;
+            } else if (MODE == FM_VCYCLE_DOWN) {
+                v[c] = f0 * chk::ld(fstage, FLD_PITCH + i, N, R);                      // r * omega/diag
+            } else if (MODE == FM_CG_UPDATE_JACOBI) {
+                const float rm = a.first ? f0 : fmaf(-alpha, chk::ld(fstage, 2 * FLD_PITCH + i, N, R), f0);
+                v[c] = rm * chk::ld(fstage, FLD_PITCH + i, N, R);
+            } else {
+                v[c] = a.first ? f0 : fmaf(beta, chk::ld(fstage, FLD_PITCH + i, N, R), f0);   // z + beta p
+            }
+        }
+    };
 #pragma unroll 1
     for (int iz = zb; iz < ze; ++iz) {
-        store(ring[(iz + 1) % RING], vc, vh);
+        if constexpr (FTMA) {
+            if (iz == zb) {
+                store(ring[(iz + 1) % RING], vc, vh);      // the prologue's per-thread fetch
+            } else {
+                float fc[3] = {0.f, 0.f, 0.f}, fh[3] = {0.f, 0.f, 0.f};
+                if (iz + 1 <= g.nz + 1) {                  // armed in the previous step; every thread waits
+                    if (!efail && !tc::mbar_wait_bounded(&fbar, (uint32_t)(iz - 1 - zb) & 1u, EPI_WAIT_NS)) {
+                        efail = 1;
+                        if (a.err) atomicExch(a.err, 1);
+                    }
+                    form(pc, fc);
+                    if (tid < NHALO) form(ph, fh);
+                }
+                store(ring[(iz + 1) % RING], fc, fh);
+            }
+        } else {
+            store(ring[(iz + 1) % RING], vc, vh);
+        }
         __syncthreads();
+        if constexpr (FTMA) {
+            // plane iz + 2, read at the top of the next step (armed only when that step exists)
+            if (tid == EPI_ISSUER && !efail && iz + 1 < ze && iz + 2 <= g.nz + 1) {
+                fence_proxy_async_cta();
+                mbar_expect_tx(&fbar, (uint32_t)(nfa * FLD_BOX * 4));
+                for (int j = 0; j < nfa; ++j)
+                    tma_load_plane(fstage + j * FLD_PITCH, &em.f[j], y0, x0, iz + 3, &fbar);
+            }
+        }
         if constexpr (TMA) {
             if (tid == EPI_ISSUER && !efail) {
                 // the previous plane's copies have landed long ago; waiting for
@@ -276,7 +346,7 @@ __global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? (TMA ? 4 : 3
                 }
             }
         }
-        if (iz + 2 <= g.nz + 1) fetch(iz + 2, vc, vh);
+        if (!FTMA && iz + 2 <= g.nz + 1) fetch(iz + 2, vc, vh);
         const uint32_t f = f_next, e8 = e8_next;
         if (own && iz + 1 < ze) {
             f_next = chk::ld(L.nflag, cbase + (iz + 1) * sz, g.slots, chk::FINE_FLAGS);
@@ -413,48 +483,74 @@ static EncodeTiledFn tensor_map_encoder() {
 
 // (y, x, z, component) view of one dense-slot vector: strides py, py*px and
 // the component plane (all multiples of 32 bytes: py is a multiple of 8);
-// the box is one tile plane, and boxes over the grid edge read zeros; the
-// 128-byte swizzle spreads the stage's 8 x 4 node patches over the banks
-static bool encode_plane_map(CUtensorMap* m, const Grid& g, const float* base) {
+// boxes over the grid edge read zeros.  The CG update's stage: one tile plane
+// (32 x 8) with the 128-byte swizzle, which spreads its 8 x 4 node patches
+// over the banks; the field stage: the tile plane with its halo (40 x 10, from
+// y0 - 4 and x0 - 1), unswizzled.
+static bool encode_plane_map(CUtensorMap* m, const Grid& g, const float* base, bool field) {
     const EncodeTiledFn fn = tensor_map_encoder();
     if (!fn || !base || (reinterpret_cast<uintptr_t>(base) & 15)) return false;
     const cuuint64_t dim[4] = {(cuuint64_t)g.py, (cuuint64_t)g.px, (cuuint64_t)g.pz, 3};
     const cuuint64_t stride[3] = {(cuuint64_t)g.py * 4, (cuuint64_t)g.py * g.px * 4, (cuuint64_t)g.slots * 4};
-    const cuuint32_t box[4] = {TY, TX, 1, 3};
+    const cuuint32_t box_epi[4] = {TY, TX, 1, 3}, box_fld[4] = {RP, HX, 1, 3};
     const cuuint32_t es[4] = {1, 1, 1, 1};
-    return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<float*>(base), dim, stride, box, es,
-              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<float*>(base), dim, stride, field ? box_fld : box_epi,
+              es, CU_TENSOR_MAP_INTERLEAVE_NONE, field ? CU_TENSOR_MAP_SWIZZLE_NONE : CU_TENSOR_MAP_SWIZZLE_128B,
+              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 // GMGS_EPI_TMA=0 keeps the CG update's operands in registers (per-thread
-// loads issued before the stencil arithmetic) instead of the TMA stage
-static bool epi_tma_enabled() {
-    const char* e = std::getenv("GMGS_EPI_TMA");
+// loads issued before the stencil arithmetic) instead of the TMA stage;
+// GMGS_FIELD_TMA=0 keeps the per-thread field loads one plane ahead instead
+// of the field stage
+static bool env_on(const char* name) {
+    const char* e = std::getenv(name);
     return !(e && e[0] == '0');
+}
+
+template <int MODE, bool DEF, int STG>
+static void launch_stg(Ctx& c, dim3 grid, const FineLevel& L, const Coef32& cf, const FineArgs& a, int zc,
+                       const EpiMaps& em) {
+    size_t dyn = 0;
+    if (STG & 1) dyn += (size_t)EPI_STAGE_BYTES + 1024;
+    if (STG & 2) dyn += (size_t)field_arrays(MODE) * FLD_PITCH * 4 + ((STG & 1) ? 0 : 128);
+    // both stages with the ring exceed the default 48 KB per CTA: opt in once per kernel
+    static const cudaError_t attr =
+        dyn ? cudaFuncSetAttribute(k_fine<MODE, DEF, STG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn)
+            : cudaSuccess;
+    GMGS_CUDA(attr);
+    k_fine<MODE, DEF, STG><<<grid, dim3(TY, TX, 1), dyn, c.stream>>>(L, cf, a, zc, em);
 }
 
 template <int MODE>
 void launch_fine(Ctx& c, const FineLevel& L, const Coef32& cf, const FineArgs& a) {
     const int zc = pick_zc(L.g, c);
     dim3 grid((L.g.ny + 1 + TY - 1) / TY, (L.g.nx + 1 + TX - 1) / TX, (L.g.nz + 1 + zc - 1) / zc);
-    const dim3 blk(TY, TX, 1);
     const bool def = coef_is_default(cf);
     EpiMaps em;
     std::memset(&em, 0, sizeof(em));
-    if constexpr (MODE == FM_CG_UPDATE_JACOBI) {
+    const float* fld[FIELD_ARRAYS] = {nullptr, nullptr, nullptr};
+    if (MODE == FM_PLAIN) fld[0] = a.v;
+    if (MODE == FM_VCYCLE_DOWN) { fld[0] = a.r32; fld[1] = a.wdinv; }
+    if (MODE == FM_CG_UPDATE_JACOBI) { fld[0] = a.r32; fld[1] = a.wdinv; fld[2] = a.q32; }
+    if (MODE == FM_CG_DIRECTION) { fld[0] = a.z32; fld[1] = a.pold; }
+    bool ftma = env_on("GMGS_FIELD_TMA");
+    for (int j = 0; j < field_arrays(MODE) && ftma; ++j) ftma = encode_plane_map(&em.f[j], L.g, fld[j], true);
+    bool etma = false;
+    if (MODE == FM_CG_UPDATE_JACOBI) {
         const float* arr[EPI_ARRAYS] = {a.r32, a.r_lo, a.x_hi, a.x_lo, a.q32, a.pold};
-        bool tma = epi_tma_enabled();
-        for (int j = 0; j < EPI_ARRAYS && tma; ++j) tma = encode_plane_map(&em.m[j], L.g, arr[j]);
-        if (tma) {
-            if (def) k_fine<MODE, true, true><<<grid, blk, EPI_DYN_SMEM, c.stream>>>(L, cf, a, zc, em);
-            else k_fine<MODE, false, true><<<grid, blk, EPI_DYN_SMEM, c.stream>>>(L, cf, a, zc, em);
-            GMGS_LAUNCHED(c);
-            return;
-        }
+        etma = env_on("GMGS_EPI_TMA");
+        for (int j = 0; j < EPI_ARRAYS && etma; ++j) etma = encode_plane_map(&em.m[j], L.g, arr[j], false);
     }
-    if (def) k_fine<MODE, true><<<grid, blk, 0, c.stream>>>(L, cf, a, zc, em);
-    else k_fine<MODE, false><<<grid, blk, 0, c.stream>>>(L, cf, a, zc, em);
+    if constexpr (MODE == FM_CG_UPDATE_JACOBI) {
+        if (etma && ftma) def ? launch_stg<MODE, true, 3>(c, grid, L, cf, a, zc, em) : launch_stg<MODE, false, 3>(c, grid, L, cf, a, zc, em);
+        else if (etma) def ? launch_stg<MODE, true, 1>(c, grid, L, cf, a, zc, em) : launch_stg<MODE, false, 1>(c, grid, L, cf, a, zc, em);
+        else if (ftma) def ? launch_stg<MODE, true, 2>(c, grid, L, cf, a, zc, em) : launch_stg<MODE, false, 2>(c, grid, L, cf, a, zc, em);
+        else def ? launch_stg<MODE, true, 0>(c, grid, L, cf, a, zc, em) : launch_stg<MODE, false, 0>(c, grid, L, cf, a, zc, em);
+    } else {
+        if (ftma) def ? launch_stg<MODE, true, 2>(c, grid, L, cf, a, zc, em) : launch_stg<MODE, false, 2>(c, grid, L, cf, a, zc, em);
+        else def ? launch_stg<MODE, true, 0>(c, grid, L, cf, a, zc, em) : launch_stg<MODE, false, 0>(c, grid, L, cf, a, zc, em);
+    }
     GMGS_LAUNCHED(c);
 }
 template void launch_fine<FM_PLAIN>(Ctx&, const FineLevel&, const Coef32&, const FineArgs&);

@@ -63,12 +63,19 @@ struct FineArgs {
     int* err = nullptr;              // set when a bounded wait for staged operands ran out
 };
 
-// TMA descriptors of FM_CG_UPDATE_JACOBI's per-node operands (r high, r low,
-// x high, x low, q, p), each a (y, x, z, component) tensor over the dense
-// slot grid with a 32 x 8 x 1 x 3 box: one tile plane of all three components.
+// TMA descriptors of the streaming kernels, each a (y, x, z, component)
+// tensor over the dense slot grid:
+//  m: FM_CG_UPDATE_JACOBI's per-node operands (r high, r low, x high, x low,
+//     q, p), a 32 x 8 x 1 x 3 box: one tile plane of all three components;
+//  f: the field inputs of the mode (FM_PLAIN v; FM_VCYCLE_DOWN r, omega/diag;
+//     FM_CG_UPDATE_JACOBI r high, omega/diag, q; FM_CG_DIRECTION z, p), a
+//     40 x 10 x 1 x 3 box: the tile plane with its one-node halo, from y - 4
+//     so that the box starts on a 16-byte boundary.
 constexpr int EPI_ARRAYS = 6;
+constexpr int FIELD_ARRAYS = 3;
 struct EpiMaps {
     CUtensorMap m[EPI_ARRAYS];
+    CUtensorMap f[FIELD_ARRAYS];
 };
 
 

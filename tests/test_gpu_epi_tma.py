@@ -1,8 +1,13 @@
-"""The CG update kernel of the mixed path with its per-node operands (r and
-x, high and low parts, q, p) staged into shared memory by TMA (fine.cu,
-k_fine<2, DEF, true>: one 32 x 8 x 3 box per array and plane, 128-byte
-swizzle, one mbarrier phase per plane) against the same kernel loading them
-into registers (GMGS_EPI_TMA=0).
+"""The streaming kernels of the mixed path with their inputs staged into
+shared memory by TMA (fine.cu, k_fine<MODE, DEF, STG>) against the same
+kernels loading them per thread into registers:
+
+* the CG update's per-node operands (r and x, high and low parts, q, p; one
+  32 x 8 x 3 box per array and plane, 128-byte swizzle), off with
+  GMGS_EPI_TMA=0;
+* every mode's field inputs with the one-node halo (r and omega/diag, q, z,
+  p; one 40 x 10 x 3 box per array and plane, unswizzled), off with
+  GMGS_FIELD_TMA=0.
 
 Both read the same values and round the same operations in the same order,
 so the mixed solve is bit-identical; the models have ragged extents (boxes
@@ -48,11 +53,11 @@ def _solve(vox, L, rho):
 
 
 @pytest.mark.parametrize("name", list(CASES))
-def test_tma_staged_update_bit_identical(name, monkeypatch):
+def test_tma_staged_inputs_bit_identical(name, monkeypatch):
     build, L, rr = CASES[name]
     vox = build()
     rho = synthetic.density(int(vox.sum()), rr, 5) if rr else None
-    switches = ("GMGS_EPI_TMA",)
+    switches = ("GMGS_EPI_TMA", "GMGS_FIELD_TMA")
     for k in switches:
         monkeypatch.setenv(k, "0")
     u0, it0, r0 = _solve(vox, L, rho)

@@ -155,16 +155,18 @@ __device__ __forceinline__ void epi_from_stage(const float* st, int sidx, bool f
     }
 }
 
-// 48 registers (5 CTAs per SM) for the stencil-only modes; the CG update
+// 48 registers (5 CTAs per SM) for the stencil-only modes, 40 (6 CTAs) for
+// the CG direction with its field staged by TMA (1.073 -> 1.063 ms; the
+// down-sweep, which also holds r for its output, spills at 40); the CG update
 // holds the state update's operands and keeps 80 registers (3 CTAs), or,
-// with the operands staged by TMA (TMA = true), 64 registers (4 CTAs; 5 CTAs
+// with the operands staged by TMA (STG bit 0), 64 registers (4 CTAs; 5 CTAs
 // at 48 registers spilled and took 2.31 ms against 1.86 ms).
 // Measured on the 153M-DOF model: 5 CTAs/SM took the down-sweep from 1.16 to
 // 1.13 ms and the direction kernel from 1.26 to 1.22 ms against 4 CTAs/SM.
 // STG bit 0: the CG update's operands staged by TMA; bit 1: the field inputs
 // staged by TMA (else loaded per thread into registers one plane ahead)
 template <int MODE, bool DEF = false, int STG = 0>
-__global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? ((STG & 1) ? 4 : 3) : 5)
+__global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? ((STG & 1) ? 4 : 3) : ((MODE == FM_CG_DIRECTION && (STG & 2)) ? 6 : 5))
     k_fine(FineLevel L, const __grid_constant__ Coef32 cf, FineArgs a, int zc, const __grid_constant__ EpiMaps em) {
     constexpr bool TMA = (STG & 1) != 0, FTMA = (STG & 2) != 0;
     static_assert(!TMA || MODE == FM_CG_UPDATE_JACOBI, "operand staging is for the CG update");

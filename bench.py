@@ -40,10 +40,10 @@ CLOCK_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.a
 
 
 # DRAM bytes (read + write) per solid node of one k_fine<FM_CG_UPDATE_JACOBI>
-# launch (its TMA-staged form): 981,097,472 B over 6,360,481 nodes in an ncu
+# launch (its TMA-staged form): 984,017,664 B over 6,360,481 nodes in an ncu
 # --set full capture of the same kernel on the same generator at half
 # resolution (--scale 0.5); the traffic grows with the node count.
-UJ_TRAFFIC_PER_NODE = 154.2
+UJ_TRAFFIC_PER_NODE = 154.7
 
 
 # Iterations the reference algorithm takes to relres < 1e-3 (omega 0.4) on the

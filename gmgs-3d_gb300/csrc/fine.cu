@@ -441,16 +441,20 @@ static int pick_zc(const Grid& g, const Ctx& c) {
     // on the 153M-DOF block, 286 -> 271 ms on kitten 512; 48 waves: slower)
     const int64_t want = (int64_t)c.num_sms * 3 * 24;
     int64_t zc = (cols * (g.nz + 1) + want - 1) / want;
-    // at least 6 planes per CTA: each chunk stages two planes beyond its own
-    // (coarse levels 22.17 -> 21.96 ms per solve against 4; 8 was slower)
-    if (zc < 6) zc = 6;
+    // at least 6 planes per CTA where that still leaves four CTAs per SM (each
+    // chunk stages two planes beyond its own: coarse levels 22.17 -> 21.96 ms
+    // per solve against 4; 8 was slower), else at least 4 (small grids keep
+    // their CTAs spread over all SMs)
+    // (the 42x37x64 model: 31.9 ms with 6 everywhere, 30.1 ms so)
+    const int64_t zmin = cols * ((g.nz + 1 + 5) / 6) < 4 * (int64_t)c.num_sms ? 4 : 6;
+    if (zc < zmin) zc = zmin;
     if (zc > 64) zc = 64;
     return (int)zc;
 }
 
 int fine_grid_blocks(const Grid& g) {
-    // upper bound over the z-chunk choices (zc >= 6)
-    return ((g.ny + 1 + TY - 1) / TY) * ((g.nx + 1 + TX - 1) / TX) * ((g.nz + 1 + 5) / 6);
+    // upper bound over the z-chunk choices (zc >= 4)
+    return ((g.ny + 1 + TY - 1) / TY) * ((g.nx + 1 + TX - 1) / TX) * ((g.nz + 1 + 3) / 4);
 }
 
 // true when cf holds exactly the compiled-in default-material tables (then

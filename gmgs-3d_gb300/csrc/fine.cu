@@ -434,12 +434,12 @@ __global__ void __launch_bounds__(NT, MODE == FM_CG_UPDATE_JACOBI ? ((STG & 1) ?
     if (MODE == FM_CG_DIRECTION || MODE == FM_CG_UPDATE_JACOBI) grid_dot_finish(dot.value(), a.dot, sh);
 }
 
-static int pick_zc(const Grid& g, const Ctx& c) {
+static int pick_zc(const Grid& g, const Ctx& c, int per_sm = 3) {
     const int64_t cols = (int64_t)((g.ny + 1 + TY - 1) / TY) * ((g.nx + 1 + TX - 1) / TX);
     // ~24 waves of 3 resident CTAs: shorter z-chunks balance the tail and let
     // empty column tiles of real geometry skip more (12 waves: 214 -> 208 ms
     // on the 153M-DOF block, 286 -> 271 ms on kitten 512; 48 waves: slower)
-    const int64_t want = (int64_t)c.num_sms * 3 * 24;
+    const int64_t want = (int64_t)c.num_sms * per_sm * 24;
     int64_t zc = (cols * (g.nz + 1) + want - 1) / want;
     // at least 6 planes per CTA where that still leaves four CTAs per SM (each
     // chunk stages two planes beyond its own: coarse levels 22.17 -> 21.96 ms
@@ -530,7 +530,10 @@ static void launch_stg(Ctx& c, dim3 grid, const FineLevel& L, const Coef32& cf, 
 
 template <int MODE>
 void launch_fine(Ctx& c, const FineLevel& L, const Coef32& cf, const FineArgs& a) {
-    const int zc = pick_zc(L.g, c);
+    // the CG update with its staged operands: longer z-chunks (2 instead of 3
+    // in the wave count: 1.820 -> 1.792 ms, 1 gave 1.820 ms; the other modes
+    // were slower with 2)
+    const int zc = pick_zc(L.g, c, MODE == FM_CG_UPDATE_JACOBI ? 2 : 3);
     dim3 grid((L.g.ny + 1 + TY - 1) / TY, (L.g.nx + 1 + TX - 1) / TX, (L.g.nz + 1 + zc - 1) / zc);
     const bool def = coef_is_default(cf);
     EpiMaps em;

@@ -4,9 +4,13 @@
 // with a four-plane ring of the input field (plus a one-node halo) in shared
 // memory.  The field is formed while staging from the kernel's inputs (the
 // Jacobi step omega*D^-1 r, or the CG direction z + beta p), so no
-// intermediate vector goes through HBM.  The plane two steps ahead and the
-// per-node data of the next plane are loaded into registers while the current
-// plane is computed, so global loads overlap the stencil arithmetic.
+// intermediate vector goes through HBM.  The field inputs of the plane two
+// steps ahead (with the halo) and, in the CG update, the per-node operands of
+// the current plane are copied into shared-memory stages by TMA
+// (cp.async.bulk.tensor, one thread per CTA, mbarrier completion) while the
+// current plane is computed, so the loads overlap the stencil arithmetic
+// without holding registers; the per-thread register form of both remains
+// (GMGS_FIELD_TMA=0, GMGS_EPI_TMA=0, or no tensor-map encoder in the driver).
 //
 // Interior nodes (all 8 surrounding elements carry the level's uniform
 // matrix) use the assembled 27-point stencil in second-difference form

@@ -34,6 +34,7 @@
 // 1/64 of its FP32 rate: in FP64 the five operations per DOF of the state
 // update kept that pipe 53 % busy and the kernel at 2.41 ms on the 153M-DOF
 // model.)
+#include <atomic>
 #include <cstring>
 
 #include "element_host.h"
@@ -524,11 +525,20 @@ static void launch_stg(Ctx& c, dim3 grid, const FineLevel& L, const Coef32& cf, 
     size_t dyn = 0;
     if (STG & 1) dyn += (size_t)EPI_STAGE_BYTES + 1024;
     if (STG & 2) dyn += (size_t)field_arrays(MODE) * FLD_PITCH * 4 + ((STG & 1) ? 0 : 128);
-    // both stages with the ring exceed the default 48 KB per CTA: opt in once per kernel
-    static const cudaError_t attr =
-        dyn ? cudaFuncSetAttribute(k_fine<MODE, DEF, STG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn)
-            : cudaSuccess;
-    GMGS_CUDA(attr);
+    // both stages with the ring exceed the default 48 KB per CTA: opt in once
+    // per kernel and device (the attribute belongs to the device's context;
+    // the first launch on a device is eager, before any graph capture)
+    if (dyn + sizeof(float) * RING * 3 * PLANE > 48 * 1024) {
+        static std::atomic<unsigned long long> opted{0};
+        int dev = 0;
+        GMGS_CUDA(cudaGetDevice(&dev));
+        const unsigned long long bit = 1ull << (dev & 63);
+        if (!(opted.load() & bit)) {
+            GMGS_CUDA(cudaFuncSetAttribute(k_fine<MODE, DEF, STG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)dyn));
+            opted.fetch_or(bit);
+        }
+    }
     k_fine<MODE, DEF, STG><<<grid, dim3(TY, TX, 1), dyn, c.stream>>>(L, cf, a, zc, em);
 }
 

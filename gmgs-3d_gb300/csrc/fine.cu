@@ -36,6 +36,7 @@
 // model.)
 #include <atomic>
 #include <cstring>
+#include <type_traits>
 
 #include "element_host.h"
 #include "fine.cuh"
@@ -565,14 +566,21 @@ void launch_fine(Ctx& c, const FineLevel& L, const Coef32& cf, const FineArgs& a
         etma = env_on("GMGS_EPI_TMA");
         for (int j = 0; j < EPI_ARRAYS && etma; ++j) etma = encode_plane_map(&em.m[j], L.g, arr[j], false);
     }
+    // the per-node operand stage exists for the CG update only
+    const int stg = (etma ? 1 : 0) | (ftma ? 2 : 0);
+    auto go = [&](auto tag) {
+        constexpr int G = decltype(tag)::value;
+        if (def) launch_stg<MODE, true, G>(c, grid, L, cf, a, zc, em);
+        else launch_stg<MODE, false, G>(c, grid, L, cf, a, zc, em);
+    };
     if constexpr (MODE == FM_CG_UPDATE_JACOBI) {
-        if (etma && ftma) def ? launch_stg<MODE, true, 3>(c, grid, L, cf, a, zc, em) : launch_stg<MODE, false, 3>(c, grid, L, cf, a, zc, em);
-        else if (etma) def ? launch_stg<MODE, true, 1>(c, grid, L, cf, a, zc, em) : launch_stg<MODE, false, 1>(c, grid, L, cf, a, zc, em);
-        else if (ftma) def ? launch_stg<MODE, true, 2>(c, grid, L, cf, a, zc, em) : launch_stg<MODE, false, 2>(c, grid, L, cf, a, zc, em);
-        else def ? launch_stg<MODE, true, 0>(c, grid, L, cf, a, zc, em) : launch_stg<MODE, false, 0>(c, grid, L, cf, a, zc, em);
+        if (stg == 3) go(std::integral_constant<int, 3>{});
+        else if (stg == 1) go(std::integral_constant<int, 1>{});
+        else if (stg == 2) go(std::integral_constant<int, 2>{});
+        else go(std::integral_constant<int, 0>{});
     } else {
-        if (ftma) def ? launch_stg<MODE, true, 2>(c, grid, L, cf, a, zc, em) : launch_stg<MODE, false, 2>(c, grid, L, cf, a, zc, em);
-        else def ? launch_stg<MODE, true, 0>(c, grid, L, cf, a, zc, em) : launch_stg<MODE, false, 0>(c, grid, L, cf, a, zc, em);
+        if (ftma) go(std::integral_constant<int, 2>{});
+        else go(std::integral_constant<int, 0>{});
     }
     GMGS_LAUNCHED(c);
 }
